@@ -1,0 +1,182 @@
+/*
+ * lyem.h -- C ABI of the GB300 raycasting + frequency-domain propagation library
+ * (liblyem_gpu.so, built from lyceanem-python_gb300/csrc).
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns
+ * an int status (LYEM_OK = 0).  No entry point calls exit() or traps the GPU.
+ *
+ * Two families:
+ *   lyem_*     device-pointer entry points, stream-ordered on the cudaStream_t
+ *              passed as `stream` (NULL = legacy default stream).  They never
+ *              allocate: scratch space is passed in by the caller, sized by the
+ *              matching *_workspace() query.
+ *   lyem_em_*  host-buffer mirrors of the four functions of the reference's
+ *              pybind11 module `lyceanem.em` (lyceanem/src/frequency_domain_models.cu:314-320):
+ *              same arguments in the same order, host arrays in, host array
+ *              out, synchronous.  They allocate and free device memory per
+ *              call, as the reference does.
+ *
+ * Layouts: points are [n,3] float32; complex 3-vectors are [n,6] float32
+ * interleaved (x.re, x.im, y.re, y.im, z.re, z.im), which is numpy/torch
+ * complex64 [n,3]; packed triangles are [n_tris,12] float32 (v0, 0, e1, 0,
+ * e2, 0) with e1 = v1 - v0, e2 = v2 - v0.
+ */
+#ifndef LYEM_H_
+#define LYEM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LYEM_API __attribute__((visibility("default")))
+#else
+#define LYEM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    LYEM_OK = 0,
+    LYEM_ERR_INVALID = 1,  /* bad argument: null pointer, negative or inconsistent size */
+    LYEM_ERR_CUDA = 2,     /* a CUDA runtime call failed (see lyem_last_cuda_error) */
+    LYEM_ERR_NOMEM = 3,    /* device allocation failed (lyem_em_* only) */
+    LYEM_ERR_TIMEOUT = 4,  /* a bounded device-side wait expired */
+    LYEM_ERR_OVERFLOW = 5, /* a size exceeds the 32-bit index range of a buffer */
+    LYEM_ERR_WORKSPACE = 6 /* workspace smaller than the *_workspace() query */
+};
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+LYEM_API int lyem_version(void);
+/* Static description of a status code. */
+LYEM_API const char *lyem_status_string(int status);
+/* cudaError_t of the last failing CUDA call made by this library (0 if none). */
+LYEM_API int lyem_last_cuda_error(void);
+/* Synchronises `stream`, then reads and clears the library's device error word
+ * (bit 0: a bounded wait expired; bit 1: an index check failed).  Returns
+ * LYEM_ERR_TIMEOUT if bit 0 was set. */
+LYEM_API int lyem_device_errors(void *stream, uint32_t *flags_out);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* Packs a triangle mesh into [n_tris,12] float32 (v0, e1, e2).
+ * Replaces the per-test vertex gather tri_vertex[idx.y] - tri_vertex[idx.x]
+ * (lyceanem/src/raycasting_brute_force.cuh:39-43) and convertTriangles
+ * (lyceanem/raycasting/rayfunctions.py:531-557).  Index values are checked;
+ * an out-of-range index sets device error bit 1 and packs a degenerate triangle. */
+LYEM_API int lyem_pack_triangles(const float *d_verts, int64_t n_verts, const int32_t *d_idx, int64_t n_tris,
+                                 float *d_tris, void *stream);
+
+/* Axis-aligned bounds of packed triangles: d_bounds6 = (xmin, ymin, zmin, xmax, ymax, zmax).
+ * Replaces the host min/max of Tile_acceleration_structure.__init__
+ * (lyceanem/models/acceleration_structures.py:55-61). */
+LYEM_API int lyem_tris_bounds(const float *d_tris, int64_t n_tris, float *d_bounds6, void *stream);
+
+/* Host helper: grid geometry for packed-triangle bounds.  cell <= 0 picks a
+ * cell size giving about two cells per triangle.  The box is the bounds
+ * padded by 2*pad (pad = 1e-3*cell). */
+LYEM_API int lyem_grid_plan(const float *bounds6, int64_t n_tris, float cell, float *origin3_out,
+                            float *cell_out, int32_t *dims3_out);
+
+/* Uniform-grid build, phase 1: per-triangle reference counts over the cells
+ * its padded box overlaps, and their exclusive scan (d_tri_offsets has
+ * n_tris+1 entries; d_tri_offsets[n_tris] is the total).  d_total_refs (one
+ * int64) receives the exact 64-bit total.  Replaces triangle_counter_kernel /
+ * count_triangles_in_bin (lyceanem/src/terrain_acceleration_build.cuh:57-134, 287-293)
+ * without its device asserts. */
+LYEM_API size_t lyem_grid_count_workspace(int64_t n_tris);
+LYEM_API int lyem_grid_count(const float *d_tris, int64_t n_tris, const float *origin3, float cell,
+                             const int32_t *dims3, int32_t *d_tri_offsets, int64_t *d_total_refs, void *d_ws,
+                             size_t ws_bytes, void *stream);
+
+/* Uniform-grid build, phase 2: emits (cell, triangle) keys, radix-sorts them
+ * by cell (stable, so triangles are ascending within a cell), writes the cell
+ * ranges d_cell_start[ncells+1] and the triangles in cell order
+ * d_cell_tris[n_refs,12].  Replaces bin_triangles_kernel_precounted /
+ * compute_bin_offsets / insert_triangle_in_bin
+ * (lyceanem/src/terrain_acceleration_build.cuh:135-205, 349-368) and the host
+ * prefix sum of lyceanem/src/frequency_domain_models.cu:118-123. */
+LYEM_API size_t lyem_grid_fill_workspace(int64_t n_refs, int64_t n_cells);
+LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *origin3, float cell,
+                            const int32_t *dims3, const int32_t *d_tri_offsets, int64_t n_refs,
+                            int32_t *d_cell_start, float *d_cell_tris, void *d_ws, size_t ws_bytes, void *stream);
+
+/* ------------------------------------------------------------- pair stage */
+
+/* Visibility + fused field for every (source n, sink m) pair:
+ *   sink_out[m, c] (+)= sum_n W[n, c] * S[n, m, c]
+ * with S[n, m, :] = vis(n, m) * em_wave(ray n->m) (lyceanem/src/em.cuh:64-120),
+ * W = d_src_W or 1.  Visibility is the Moller-Trumbore any-hit test of
+ * lyceanem/src/raycasting.cuh:19-68 (cull = 1) or the numba engine's
+ * lyceanem/raycasting/rayfunctions.py:37-104 (cull = 0, eps = 1e-7) against all
+ * packed triangles (brute force, d_cell_start == NULL) or a grid from
+ * lyem_grid_fill.  self_to_self = 0 reproduces the reference's skip of the pair
+ * whose source index equals its sink index (lyceanem/src/raycasting_brute_force.cuh:27).
+ * Replaces raycast_brute_force / raycast_tiles + set_values + points_to_rays
+ * (lyceanem/src/raycasting_brute_force.cuh:68-88, raycasting_accelerated.cuh:458-482,
+ * raycasting.cuh:80-108) and the host sum over sources
+ * (lyceanem/models/frequency_domain.py:847-849).
+ * Optional outputs (NULL to skip): d_pair_out [n_src, n_snk, 6] (the
+ * reference's scattering network layout, zero for blocked pairs), d_mask_bits
+ * [n_src, ceil(n_snk/32)] uint32 (bit m%32 of word m/32 = visible),
+ * d_counters uint64[2] incremented by (visible pairs, ray/triangle tests).
+ * src_chunk: sources per thread block (0 = automatic). */
+LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
+                                          int32_t src_chunk);
+LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const float *d_src_W, int64_t n_src,
+                             const float *d_snk_pos, const float *d_snk_nrm, int64_t n_snk, const float *d_tris,
+                             int64_t n_tris, const int32_t *d_cell_start, const float *d_cell_tris,
+                             const float *grid_origin3, float grid_cell, const int32_t *grid_dims3, double alpha,
+                             double beta, int32_t self_to_self, int32_t cull, float eps, float *d_sink_out,
+                             int32_t accumulate, float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
+                             int32_t src_chunk, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Expands a bit mask [n_src, ceil(n_snk/32)] to bytes [n_src, n_snk] (0/1). */
+LYEM_API int lyem_mask_to_bytes(const uint32_t *d_mask_bits, int64_t n_src, int64_t n_snk, uint8_t *d_out,
+                                void *stream);
+
+/* ------------------------------------------ host mirrors of lyceanem.em */
+
+/* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):
+ * triangles binned over the y-z grid of ncells_x (along y) by ncells_y
+ * (along z) square cells of width cell_width from (ymin, z_min); cell index
+ * iy*ncells_y + iz.  Every cell a triangle's y-z box overlaps receives it
+ * (the reference bins vertex cells plus one corner and asserts adjacency). */
+LYEM_API int lyem_em_bin_counts(const float *tri_vertex, int64_t n_vertex, const int32_t *tri_index, int64_t n_tris,
+                                int32_t ncells_x, int32_t ncells_y, float ymin, float cell_width, float z_min,
+                                int32_t *counts_out);
+
+/* bin_triangles_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:370-431):
+ * the vertex-index triples of the binned triangles in cell order, triangles
+ * ascending within a cell; out has 3*sum_bin_counts entries. */
+LYEM_API int lyem_em_bin_triangles(const float *tri_vertex, int64_t n_vertex, const int32_t *tri_index,
+                                   int64_t n_tris, int32_t ncells_x, int32_t ncells_y, float ymin, float cell_width,
+                                   float z_min, const int32_t *bin_counts, int64_t sum_bin_counts, int32_t *out);
+
+/* calculate_scattering_brute_force (lyceanem/src/frequency_domain_models.cu:190-311),
+ * returning the network the reference computes (its binding never copies it
+ * back): out[n_source*n_end*6] float32. */
+LYEM_API int lyem_em_calculate_scattering_brute_force(
+    const float *source, int64_t n_source, const float *end, int64_t n_end, const int32_t *triangles, int64_t n_tris,
+    const float *triangle_vertex, int64_t n_vertex, float wave_length, const float *ex_real, const float *ex_imag,
+    const float *ey_real, const float *ey_imag, const float *ez_real, const float *ez_imag, const float *normal,
+    float alpha, float beta, int32_t not_self_to_self, float *out);
+
+/* calculate_scattering_tiles (lyceanem/src/frequency_domain_models.cu:44-187):
+ * the triangle set is the distinct vertex triples of bin_triangles; the
+ * traversal uses this library's own uniform grid, so bounds, tile size and
+ * bin counts only describe the caller's binning.  out[n_source*n_end*6]. */
+LYEM_API int lyem_em_calculate_scattering_tiles(
+    const float *source, int64_t n_source, const float *end, int64_t n_end, const float *triangle_vertex,
+    int64_t n_vertex, float wave_length, const float *ex_real, const float *ex_imag, const float *ey_real,
+    const float *ey_imag, const float *ez_real, const float *ez_imag, const float *normal, float xmin, float xmax,
+    float ymin, float ymax, float zmin, float zmax, float tile_size, const int32_t *bin_count,
+    const int32_t *bin_triangles, int32_t n_cellsx, int32_t n_cellsy, int32_t binned_tri_num, float alpha,
+    float beta, int32_t not_self_to_self, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LYEM_H_ */

@@ -1,0 +1,219 @@
+// lyem_device.cuh -- device arithmetic shared by every kernel of the library.
+//
+// Visibility arithmetic is fully specified: each operation is an IEEE binary32
+// operation with round-to-nearest, written with the __f*_rn intrinsics so the
+// compiler can neither contract nor reorder it.  The CPU oracle performs the
+// same sequence with fmaf() under -ffp-contract=off, so masks agree bit for
+// bit.  The operation order follows the reference formulas:
+//   points_to_rays   lyceanem/src/raycasting.cuh:80-95
+//   hit              lyceanem/src/raycasting.cuh:19-68 (cull) and
+//                    lyceanem/raycasting/rayfunctions.py:37-104 (no cull)
+//   cross/dot        contracted as fma(a, b, -(c*d)) and fma(z, z, fma(y, y, x*x))
+// The reference computes F = 1.0/A in double and rounds to float; with a
+// 53-bit intermediate for a 24-bit quotient that double rounding is innocuous,
+// so F equals the correctly rounded FP32 reciprocal __frcp_rn(A).
+//
+// The field follows em_wave/ray_launch (lyceanem/src/em.cuh:18-120) in FP32
+// except the phase beta*r, which is formed from FP64 differences of the input
+// coordinates and reduced modulo 2*pi in FP64 before the FP32 sincos.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lyem {
+
+constexpr float kEpsilon = 0.000001f;  // lyceanem/src/math_utility.cuh:9
+
+struct Ray {
+    float dx, dy, dz, len;
+};
+
+__device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float ex, float ey, float ez) {
+    float rx = __fsub_rn(ex, ox), ry = __fsub_rn(ey, oy), rz = __fsub_rn(ez, oz);
+    float w2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+    float w = __fsqrt_rn(w2);
+    Ray r;
+    r.dx = __fdiv_rn(rx, w);
+    r.dy = __fdiv_rn(ry, w);
+    r.dz = __fdiv_rn(rz, w);
+    r.len = w;
+    return r;
+}
+
+// Per (source, triangle) quantities of the Moller-Trumbore test that do not
+// depend on the ray direction: tvec = o - v0, qvec = tvec x e1, tq = e2 . qvec.
+// Computing them once per source and reusing them gives the same bits as
+// recomputing them per test.
+struct TriPre {
+    float4 a;  // e1.x e1.y e1.z e2.x
+    float4 b;  // e2.y e2.z t.x t.y
+    float4 c;  // t.z q.x q.y q.z
+    float4 d;  // tq  -    -   -
+};
+
+__device__ __forceinline__ TriPre make_tripre(float ox, float oy, float oz, float4 v0, float4 e1, float4 e2) {
+    float tx = __fsub_rn(ox, v0.x), ty = __fsub_rn(oy, v0.y), tz = __fsub_rn(oz, v0.z);
+    float qx = __fmaf_rn(ty, e1.z, -__fmul_rn(tz, e1.y));
+    float qy = __fmaf_rn(tz, e1.x, -__fmul_rn(tx, e1.z));
+    float qz = __fmaf_rn(tx, e1.y, -__fmul_rn(ty, e1.x));
+    float tq = __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx)));
+    TriPre p;
+    p.a = make_float4(e1.x, e1.y, e1.z, e2.x);
+    p.b = make_float4(e2.y, e2.z, tx, ty);
+    p.c = make_float4(tz, qx, qy, qz);
+    p.d = make_float4(tq, 0.f, 0.f, 0.f);
+    return p;
+}
+
+template <bool CULL>
+__device__ __forceinline__ bool det_rejects(float A, float eps) {
+    if (CULL) return !(A >= eps);  // |A| < eps or A < 0 (NaN also rejected; the reference returns 0 for it later)
+    return fabsf(A) < eps;
+}
+
+// hit() with the per-source quantities precomputed.
+template <bool CULL>
+__device__ __forceinline__ bool hit_pre(const Ray& r, const TriPre& p, float eps) {
+    const float e1x = p.a.x, e1y = p.a.y, e1z = p.a.z;
+    const float e2x = p.a.w, e2y = p.b.x, e2z = p.b.y;
+    float px = __fmaf_rn(r.dy, e2z, -__fmul_rn(r.dz, e2y));
+    float py = __fmaf_rn(r.dz, e2x, -__fmul_rn(r.dx, e2z));
+    float pz = __fmaf_rn(r.dx, e2y, -__fmul_rn(r.dy, e2x));
+    float A = __fmaf_rn(e1z, pz, __fmaf_rn(e1y, py, __fmul_rn(e1x, px)));
+    if (det_rejects<CULL>(A, eps)) return false;
+    float F = __frcp_rn(A);
+    float U = __fmul_rn(F, __fmaf_rn(p.c.x, pz, __fmaf_rn(p.b.w, py, __fmul_rn(p.b.z, px))));
+    if (U < 0.f || U > 1.f) return false;
+    float V = __fmul_rn(F, __fmaf_rn(r.dz, p.c.w, __fmaf_rn(r.dy, p.c.z, __fmul_rn(r.dx, p.c.y))));
+    if (V < 0.f || __fadd_rn(U, V) > 1.f) return false;
+    float t = __fmul_rn(F, p.d.x);
+    const float two_eps = 2.f * eps;
+    return (t > two_eps) && (t < __fsub_rn(r.len, two_eps));
+}
+
+// hit() from the packed triangle (v0, e1, e2) and the ray origin.
+template <bool CULL>
+__device__ __forceinline__ bool hit_full(const Ray& r, float ox, float oy, float oz, float4 v0, float4 e1,
+                                         float4 e2, float eps) {
+    float px = __fmaf_rn(r.dy, e2.z, -__fmul_rn(r.dz, e2.y));
+    float py = __fmaf_rn(r.dz, e2.x, -__fmul_rn(r.dx, e2.z));
+    float pz = __fmaf_rn(r.dx, e2.y, -__fmul_rn(r.dy, e2.x));
+    float A = __fmaf_rn(e1.z, pz, __fmaf_rn(e1.y, py, __fmul_rn(e1.x, px)));
+    if (det_rejects<CULL>(A, eps)) return false;
+    float tx = __fsub_rn(ox, v0.x), ty = __fsub_rn(oy, v0.y), tz = __fsub_rn(oz, v0.z);
+    float F = __frcp_rn(A);
+    float U = __fmul_rn(F, __fmaf_rn(tz, pz, __fmaf_rn(ty, py, __fmul_rn(tx, px))));
+    if (U < 0.f || U > 1.f) return false;
+    float qx = __fmaf_rn(ty, e1.z, -__fmul_rn(tz, e1.y));
+    float qy = __fmaf_rn(tz, e1.x, -__fmul_rn(tx, e1.z));
+    float qz = __fmaf_rn(tx, e1.y, -__fmul_rn(ty, e1.x));
+    float V = __fmul_rn(F, __fmaf_rn(r.dz, qz, __fmaf_rn(r.dy, qy, __fmul_rn(r.dx, qx))));
+    if (V < 0.f || __fadd_rn(U, V) > 1.f) return false;
+    float t = __fmul_rn(F, __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx))));
+    const float two_eps = 2.f * eps;
+    return (t > two_eps) && (t < __fsub_rn(r.len, two_eps));
+}
+
+// Path length in FP64 from the FP32 end points: the coordinate differences are
+// exact in FP64, and one Newton step from the FP32 length w gives a relative
+// error far below 1e-12.
+__device__ __forceinline__ double path_length_fp64(float ox, float oy, float oz, float ex, float ey, float ez,
+                                                   float w) {
+    double dx = (double)ex - (double)ox;
+    double dy = (double)ey - (double)oy;
+    double dz = (double)ez - (double)oz;
+    double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    double wd = (double)w;
+    double h = (double)(0.5f * __frcp_rn(w));
+    return fma(fma(-wd, wd, r2), h, wd);
+}
+
+// beta * r reduced to [-pi, pi] in FP64 (Cody-Waite with a two-term 2*pi).
+__device__ __forceinline__ float reduced_phase(double beta, double r) {
+    const double kTwoPiHi = 6.283185307179586232;      // nearest double to 2*pi
+    const double kTwoPiLo = 2.4492935982947064e-16;    // 2*pi - kTwoPiHi
+    const double kInvTwoPi = 0.15915494309189534561;
+    double ph = beta * r;
+    double k = rint(ph * kInvTwoPi);
+    double red = fma(-k, kTwoPiHi, ph);
+    red = fma(-k, kTwoPiLo, red);
+    return (float)red;
+}
+
+// Field of one visible pair: E_L * loss with
+//   E_L  = E - (E.d) d  (= (E.u)u + (E.v)v of ray_launch, em.cuh:18-61)
+//   G    = exp(-alpha r)/r * exp(-j beta r);  dG = (-alpha - 1/r - j beta) G
+//   loss = -(1/(2 pi)) dG (n_sink . d)        (em.cuh:64-120)
+// E and out are complex 3-vectors as 6 floats (re, im) x (x, y, z).
+__device__ __forceinline__ void pair_field(const Ray& r, double rlen, const float* E, float nx, float ny, float nz,
+                                           float alpha, float beta_f, double beta_d, float* out) {
+    float ph = reduced_phase(beta_d, rlen);
+    float s, c;
+    sincosf(ph, &s, &c);
+    float inv_r = 1.0f / r.len;
+    float mag = expf(-alpha * r.len) * inv_r;
+    float g_re = mag * c, g_im = -mag * s;
+    float a_re = -alpha - inv_r, a_im = -beta_f;
+    float dg_re = a_re * g_re - a_im * g_im;
+    float dg_im = a_re * g_im + a_im * g_re;
+    float nd = nx * r.dx + ny * r.dy + nz * r.dz;
+    const float front = -0.15915494309189535f;  // -1/(2 pi)
+    float l_re = front * nd * dg_re, l_im = front * nd * dg_im;
+    float ed_re = E[0] * r.dx + E[2] * r.dy + E[4] * r.dz;
+    float ed_im = E[1] * r.dx + E[3] * r.dy + E[5] * r.dz;
+    float el_re[3] = {E[0] - ed_re * r.dx, E[2] - ed_re * r.dy, E[4] - ed_re * r.dz};
+    float el_im[3] = {E[1] - ed_im * r.dx, E[3] - ed_im * r.dy, E[5] - ed_im * r.dz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        out[2 * k] = el_re[k] * l_re - el_im[k] * l_im;
+        out[2 * k + 1] = el_re[k] * l_im + el_im[k] * l_re;
+    }
+}
+
+// Bounded wait on an mbarrier phase.  Returns false if the deadline (in SM
+// clock cycles) passes first; the caller then reports LYEM_ERR_TIMEOUT.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar_addr, uint32_t parity, long long max_cycles) {
+    long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mbar_addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > max_cycles) return false;
+    }
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar_addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar_addr), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// One-dimensional TMA bulk copy global -> shared, completing on an mbarrier.
+// dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void tma_load_1d(uint32_t dst_smem, const void* src_gmem, uint32_t bytes,
+                                            uint32_t mbar_addr) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar_addr), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst_smem),
+        "l"(src_gmem), "r"(bytes), "r"(mbar_addr)
+        : "memory");
+}
+
+}  // namespace lyem

@@ -1,0 +1,67 @@
+// lyem_internal.cuh -- parameter blocks and host helpers shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lyem.h"
+
+namespace lyem {
+
+// Bounded device waits give up after this many SM cycles (about one second at
+// GB300 clocks) and raise LYEM_ERR_TIMEOUT instead of hanging.
+constexpr long long kWaitCycles = 2000000000LL;
+
+// Device-wide sticky error word (bit 0: a bounded wait expired, bit 1: an index
+// check failed), defined in lyem_stage.cu.  Kernels of other translation units
+// receive its device address from device_error_word().
+unsigned int* device_error_word();
+cudaError_t read_clear_device_errors(unsigned int* flags, cudaStream_t stream);
+
+// One "pair stage": every (source n, sink m) segment is tested for visibility
+// against the scene; visible pairs contribute their field to sink m.
+//   out[m, c] (+)= sum_n W[n, c] * S[n, m, c]      (W == nullptr means 1)
+// Optional outputs: the full per-pair network S (the reference's layout,
+// source-major, 6 floats per pair) and a bit mask of visible pairs.
+struct StageParams {
+    const float* src_pos;  // [n_src, 3]
+    const float* src_E;    // [n_src, 6] complex excitation (re, im) x (x, y, z)
+    const float* src_W;    // [n_src, 6] per-component output weights or nullptr
+    long long n_src;
+    const float* snk_pos;  // [n_snk, 3]
+    const float* snk_nrm;  // [n_snk, 3]
+    long long n_snk;
+    // brute force
+    const float4* tris;  // [n_tris, 3] float4 (v0, e1, e2)
+    long long n_tris;
+    // uniform grid (used when cell_start != nullptr)
+    const int* cell_start;     // [ncells + 1]
+    const float4* cell_tris;   // [n_refs, 3] float4, triangles in cell order
+    float g0[3], g1[3];        // grid box
+    float cell, inv_cell;
+    int dims[3];
+    // physics
+    float alpha, beta_f;
+    double beta_d;
+    float eps;
+    int skip_diag;
+    // launch shape
+    int src_chunk;
+    // outputs
+    float* partial;              // [n_chunks, n_snk, 6]
+    float* pair_out;             // [n_src, n_snk, 6] or nullptr
+    unsigned int* mask_bits;     // [n_src, mask_words] or nullptr
+    long long mask_words;
+    unsigned long long* counters;  // [0] visible pairs, [1] ray/triangle tests (may be nullptr)
+};
+
+// Host-side launchers (lyem_stage.cu).
+cudaError_t launch_pair_stage(const StageParams& p, int cull, cudaStream_t stream);
+cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, long long n_snk, float* out,
+                                   int accumulate, cudaStream_t stream);
+int stage_block_threads();
+int brute_max_src_chunk();
+
+// Grid build (lyem_grid.cu).
+cudaError_t launch_tris_bounds(const float4* tris, long long n_tris, float* bounds6, cudaStream_t stream);
+
+}  // namespace lyem

@@ -1,0 +1,387 @@
+// lyem_stage.cu -- visibility + fused field kernels ("pair stages").
+//
+// Thread block = 128 sinks (one per thread) x a chunk of sources.  Each thread
+// resolves the visibility of its sink from every source of the chunk, then
+// evaluates the field of the visible pairs and sums them over the chunk in
+// registers.  Chunk partial sums go to a [n_chunks, n_snk, 6] buffer and a
+// second kernel reduces them in FP64 in a fixed order, so results are
+// reproducible run to run.  Optionally the kernels also write the per-pair
+// network (the reference's output layout) and a visibility bit mask.
+//
+// Brute force (replaces raycast_brute_force, lyceanem/src/raycasting_brute_force.cuh:68-88):
+// triangle tiles of 128 are staged in shared memory by TMA bulk copies
+// (double-buffered, mbarrier-completed, bounded waits); for each source of
+// the chunk the block derives the ray-independent part of the test once per
+// triangle (tvec, qvec, e2.qvec) and every thread tests its ray against the
+// tile.  A ray stops at its first hit; a tile step is skipped when no thread
+// of the block still has an unresolved ray (block vote), and the block stops
+// loading tiles once every ray is resolved.
+//
+// Grid (replaces raycast_tiles + DDA, lyceanem/src/raycasting_accelerated.cuh:106-268, 458-482):
+// each thread walks its segment through a uniform 3-D grid (Amanatides-Woo,
+// boundary crossings recomputed from the cell index so no error accumulates)
+// and tests the triangles stored contiguously per cell (float4 loads), stopping
+// at the first hit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lyem_device.cuh"
+#include "lyem_internal.cuh"
+
+namespace lyem {
+
+__device__ unsigned int g_device_error = 0;
+
+unsigned int* device_error_word() {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
+    return static_cast<unsigned int*>(p);
+}
+
+cudaError_t read_clear_device_errors(unsigned int* flags, cudaStream_t stream) {
+    unsigned int zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(flags, g_device_error, sizeof(unsigned int), 0,
+                                              cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyToSymbolAsync(g_device_error, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(stream);
+}
+
+constexpr int kThreads = 128;
+constexpr int kTile = 128;
+constexpr int kBruteMaxChunk = 32;
+
+int stage_block_threads() { return kThreads; }
+int brute_max_src_chunk() { return kBruteMaxChunk; }
+
+struct BruteSmem {
+    float4 raw[2][kTile * 3];
+    TriPre pre[2][kTile];
+    unsigned long long mbar[2];
+};
+
+__device__ __forceinline__ void load_E(const float* base, long long n, float* E) {
+    const float2* p = reinterpret_cast<const float2*>(base + 6 * n);
+    float2 a = p[0], b = p[1], c = p[2];
+    E[0] = a.x; E[1] = a.y; E[2] = b.x; E[3] = b.y; E[4] = c.x; E[5] = c.y;
+}
+
+// Field epilogue for one (n, m) pair shared by both kernels.
+template <bool WEIGHTED, bool PAIR_OUT>
+__device__ __forceinline__ void pair_epilogue(const StageParams& p, long long n, long long m, bool m_ok, bool vis,
+                                              float ox, float oy, float oz, float ex, float ey, float ez, float nx,
+                                              float ny, float nz, float* acc) {
+    if (vis) {
+        Ray r = make_ray(ox, oy, oz, ex, ey, ez);
+        double rl = path_length_fp64(ox, oy, oz, ex, ey, ez, r.len);
+        float E[6], out[6];
+        load_E(p.src_E, n, E);
+        pair_field(r, rl, E, nx, ny, nz, p.alpha, p.beta_f, p.beta_d, out);
+        if (PAIR_OUT) {
+            float2* po = reinterpret_cast<float2*>(p.pair_out + 6 * (n * p.n_snk + m));
+            po[0] = make_float2(out[0], out[1]);
+            po[1] = make_float2(out[2], out[3]);
+            po[2] = make_float2(out[4], out[5]);
+        }
+        if (WEIGHTED) {
+            float W[6];
+            load_E(p.src_W, n, W);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                acc[2 * k] += W[2 * k] * out[2 * k] - W[2 * k + 1] * out[2 * k + 1];
+                acc[2 * k + 1] += W[2 * k] * out[2 * k + 1] + W[2 * k + 1] * out[2 * k];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) acc[k] += out[k];
+        }
+    } else if (PAIR_OUT && m_ok) {
+        float2* po = reinterpret_cast<float2*>(p.pair_out + 6 * (n * p.n_snk + m));
+        po[0] = po[1] = po[2] = make_float2(0.f, 0.f);
+    }
+}
+
+__device__ __forceinline__ void write_mask(const StageParams& p, long long n, long long m, bool vis) {
+    unsigned b = __ballot_sync(0xffffffffu, vis);
+    long long w = m >> 5;
+    if ((threadIdx.x & 31) == 0 && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
+}
+
+__device__ __forceinline__ void flush_block(const StageParams& p, long long m, bool m_ok, const float* acc,
+                                            unsigned long long vis_count, unsigned long long tests) {
+    if (m_ok) {
+        float2* dst = reinterpret_cast<float2*>(p.partial + 6 * ((long long)blockIdx.y * p.n_snk + m));
+        dst[0] = make_float2(acc[0], acc[1]);
+        dst[1] = make_float2(acc[2], acc[3]);
+        dst[2] = make_float2(acc[4], acc[5]);
+    }
+    if (p.counters) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            vis_count += __shfl_down_sync(0xffffffffu, vis_count, o);
+            tests += __shfl_down_sync(0xffffffffu, tests, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (vis_count) atomicAdd(p.counters + 0, vis_count);
+            if (tests) atomicAdd(p.counters + 1, tests);
+        }
+    }
+}
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT>
+__global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    BruteSmem& sm = *reinterpret_cast<BruteSmem*>(smem_raw);
+
+    const int tid = threadIdx.x;
+    const long long m = (long long)blockIdx.x * kThreads + tid;
+    const bool m_ok = m < p.n_snk;
+    const long long n0 = (long long)blockIdx.y * p.src_chunk;
+    const long long rem = p.n_src - n0;
+    const int nsrc = (int)(rem < p.src_chunk ? rem : p.src_chunk);
+
+    float ex = 0.f, ey = 0.f, ez = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    if (m_ok) {
+        ex = p.snk_pos[3 * m]; ey = p.snk_pos[3 * m + 1]; ez = p.snk_pos[3 * m + 2];
+        nx = p.snk_nrm[3 * m]; ny = p.snk_nrm[3 * m + 1]; nz = p.snk_nrm[3 * m + 2];
+    }
+    uint32_t pending = 0, blocked = 0;
+    for (int s = 0; s < nsrc; ++s)
+        if (m_ok && !(p.skip_diag && n0 + s == m)) pending |= 1u << s;
+
+    const long long T = p.n_tris;
+    const int ntiles = (int)((T + kTile - 1) / kTile);
+    const uint32_t mb0 = smem_addr(&sm.mbar[0]), mb1 = smem_addr(&sm.mbar[1]);
+    if (tid == 0) {
+        mbar_init(mb0, 1);
+        mbar_init(mb1, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        long long first = (long long)k * kTile;
+        long long cnt = T - first < kTile ? T - first : kTile;
+        tma_load_1d(smem_addr(&sm.raw[k & 1][0]), p.tris + 3 * first, (uint32_t)(cnt * 48), (k & 1) ? mb1 : mb0);
+    };
+    if (tid == 0) {
+        if (ntiles > 0) issue(0);
+        if (ntiles > 1) issue(1);
+    }
+
+    unsigned long long tests = 0;
+    bool timed_out = false;
+    int k = 0;
+    for (; k < ntiles; ++k) {
+        if (!__syncthreads_or(pending != 0)) break;
+        bool ok = mbar_wait_bounded((k & 1) ? mb1 : mb0, (k >> 1) & 1, kWaitCycles);
+        if (__syncthreads_or(!ok)) { timed_out = true; break; }
+        const int cnt = (int)(T - (long long)k * kTile < kTile ? T - (long long)k * kTile : kTile);
+        const float4* rt = sm.raw[k & 1];
+        for (int s = 0; s < nsrc; ++s) {
+            TriPre* pb = sm.pre[(k * nsrc + s) & 1];
+            const float* so = p.src_pos + 3 * (n0 + s);
+            const float ox = so[0], oy = so[1], oz = so[2];
+            if (tid < cnt) pb[tid] = make_tripre(ox, oy, oz, rt[3 * tid], rt[3 * tid + 1], rt[3 * tid + 2]);
+            const bool mine = (pending >> s) & 1u;
+            if (!__syncthreads_or(mine)) continue;
+            if (mine) {
+                const Ray r = make_ray(ox, oy, oz, ex, ey, ez);
+                int j = 0;
+                bool hitany = false;
+                for (; j < cnt; ++j) {
+                    if (hit_pre<CULL>(r, pb[j], p.eps)) { hitany = true; break; }
+                }
+                tests += hitany ? (unsigned long long)(j + 1) : (unsigned long long)cnt;
+                if (hitany) {
+                    pending &= ~(1u << s);
+                    blocked |= 1u << s;
+                }
+            }
+        }
+        // Every thread has finished reading raw[k & 1] (the block vote of the
+        // last source step above is a barrier): refill it with tile k + 2.
+        if (tid == 0 && k + 2 < ntiles) {
+            fence_proxy_async_smem();
+            issue(k + 2);
+        }
+    }
+    // Wait (bounded) for copies still in flight before the block may exit.
+    {
+        int hi = k + 2 < ntiles ? k + 2 : ntiles;
+        for (int j = k; j < hi; ++j) {
+            if (timed_out && j == k) continue;
+            if (!mbar_wait_bounded((j & 1) ? mb1 : mb0, (j >> 1) & 1, kWaitCycles)) timed_out = true;
+        }
+    }
+    if (timed_out) {
+        if (tid == 0) atomicOr(&g_device_error, 1u);
+        return;
+    }
+
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    unsigned long long vis_count = 0;
+    for (int s = 0; s < nsrc; ++s) {
+        const long long n = n0 + s;
+        const bool vis = m_ok && !((blocked >> s) & 1u);
+        if (MASK_OUT) write_mask(p, n, m, vis);
+        const float* so = p.src_pos + 3 * n;
+        pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
+        vis_count += vis;
+    }
+    flush_block(p, m, m_ok, acc, vis_count, tests);
+}
+
+// Any-hit walk of the segment o -> o + len*d through the uniform grid.
+template <bool CULL>
+__device__ __forceinline__ bool grid_blocked(const StageParams& p, float ox, float oy, float oz, const Ray& r,
+                                             unsigned long long& tests) {
+    const float o[3] = {ox, oy, oz};
+    const float d[3] = {r.dx, r.dy, r.dz};
+    float inv[3];
+    float t0 = 0.f, t1 = r.len;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (d[k] == 0.f) {
+            inv[k] = 0.f;
+            if (o[k] < p.g0[k] || o[k] > p.g1[k]) return false;
+        } else {
+            inv[k] = 1.0f / d[k];
+            float ta = (p.g0[k] - o[k]) * inv[k], tb = (p.g1[k] - o[k]) * inv[k];
+            t0 = fmaxf(t0, fminf(ta, tb));
+            t1 = fminf(t1, fmaxf(ta, tb));
+        }
+    }
+    if (!(t0 <= t1)) return false;
+    int idx[3], step[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float q = (o[k] + t0 * d[k] - p.g0[k]) * p.inv_cell;
+        int i = (int)floorf(q);
+        i = i < 0 ? 0 : (i > p.dims[k] - 1 ? p.dims[k] - 1 : i);
+        idx[k] = i;
+        step[k] = d[k] > 0.f ? 1 : (d[k] < 0.f ? -1 : 0);
+    }
+    const int nx = p.dims[0], nxy = p.dims[0] * p.dims[1];
+    // A monotone walk visits at most dims[0] + dims[1] + dims[2] cells.
+    int guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
+    while (true) {
+        if (--guard < 0) {
+            atomicOr(&g_device_error, 2u);
+            return false;
+        }
+        const int c = idx[2] * nxy + idx[1] * nx + idx[0];
+        const int r0 = __ldg(p.cell_start + c), r1 = __ldg(p.cell_start + c + 1);
+        for (int q = r0; q < r1; ++q) {
+            const float4* t = p.cell_tris + 3 * (long long)q;
+            const float4 v0 = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
+            if (hit_full<CULL>(r, ox, oy, oz, v0, e1, e2, p.eps)) {
+                tests += (unsigned long long)(q - r0 + 1);
+                return true;
+            }
+        }
+        tests += (unsigned long long)(r1 - r0);
+        // parameter of the next boundary crossing on each axis, from the index
+        float tn[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (step[k] == 0) {
+                tn[k] = __int_as_float(0x7f800000);
+            } else {
+                float b = p.g0[k] + (float)(idx[k] + (step[k] > 0)) * p.cell;
+                tn[k] = (b - o[k]) * inv[k];
+            }
+        }
+        int a = (tn[0] < tn[1]) ? (tn[0] < tn[2] ? 0 : 2) : (tn[1] < tn[2] ? 1 : 2);
+        if (tn[a] > t1) return false;
+        idx[a] += step[a];
+        if (idx[a] < 0 || idx[a] >= p.dims[a]) return false;
+    }
+}
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT>
+__global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams p) {
+    const int tid = threadIdx.x;
+    const long long m = (long long)blockIdx.x * kThreads + tid;
+    const bool m_ok = m < p.n_snk;
+    const long long n0 = (long long)blockIdx.y * p.src_chunk;
+    const long long rem = p.n_src - n0;
+    const int nsrc = (int)(rem < p.src_chunk ? rem : p.src_chunk);
+    float ex = 0.f, ey = 0.f, ez = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    if (m_ok) {
+        ex = p.snk_pos[3 * m]; ey = p.snk_pos[3 * m + 1]; ez = p.snk_pos[3 * m + 2];
+        nx = p.snk_nrm[3 * m]; ny = p.snk_nrm[3 * m + 1]; nz = p.snk_nrm[3 * m + 2];
+    }
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    unsigned long long vis_count = 0, tests = 0;
+    for (int s = 0; s < nsrc; ++s) {
+        const long long n = n0 + s;
+        const float* so = p.src_pos + 3 * n;
+        const float ox = so[0], oy = so[1], oz = so[2];
+        bool vis = m_ok;
+        if (m_ok && !(p.skip_diag && n == m)) {
+            const Ray r = make_ray(ox, oy, oz, ex, ey, ez);
+            vis = !grid_blocked<CULL>(p, ox, oy, oz, r, tests);
+        }
+        if (MASK_OUT) write_mask(p, n, m, vis);
+        pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, ox, oy, oz, ex, ey, ez, nx, ny, nz, acc);
+        vis_count += vis;
+    }
+    flush_block(p, m, m_ok, acc, vis_count, tests);
+}
+
+__global__ void reduce_partials_kernel(const float* __restrict__ partial, long long n_chunks, long long n_elem,
+                                       float* __restrict__ out, int accumulate) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_elem;
+         i += (long long)gridDim.x * blockDim.x) {
+        double s = accumulate ? (double)out[i] : 0.0;
+        for (long long c = 0; c < n_chunks; ++c) s += (double)partial[c * n_elem + i];
+        out[i] = (float)s;
+    }
+}
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT>
+static cudaError_t launch_t(const StageParams& p, cudaStream_t stream) {
+    const long long chunks = (p.n_src + p.src_chunk - 1) / p.src_chunk;
+    dim3 grid((unsigned)((p.n_snk + kThreads - 1) / kThreads), (unsigned)chunks);
+    if (p.cell_start) {
+        grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT><<<grid, kThreads, 0, stream>>>(p);
+    } else {
+        const size_t smem = sizeof(BruteSmem);
+        auto kern = brute_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, kThreads, smem, stream>>>(p);
+    }
+    return cudaGetLastError();
+}
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT>
+static cudaError_t launch_m(const StageParams& p, cudaStream_t s) {
+    return p.mask_bits ? launch_t<CULL, WEIGHTED, PAIR_OUT, true>(p, s) : launch_t<CULL, WEIGHTED, PAIR_OUT, false>(p, s);
+}
+template <bool CULL, bool WEIGHTED>
+static cudaError_t launch_p(const StageParams& p, cudaStream_t s) {
+    return p.pair_out ? launch_m<CULL, WEIGHTED, true>(p, s) : launch_m<CULL, WEIGHTED, false>(p, s);
+}
+template <bool CULL>
+static cudaError_t launch_w(const StageParams& p, cudaStream_t s) {
+    return p.src_W ? launch_p<CULL, true>(p, s) : launch_p<CULL, false>(p, s);
+}
+
+cudaError_t launch_pair_stage(const StageParams& p, int cull, cudaStream_t stream) {
+    if (p.n_src == 0 || p.n_snk == 0) return cudaSuccess;
+    return cull ? launch_w<true>(p, stream) : launch_w<false>(p, stream);
+}
+
+cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, long long n_snk, float* out,
+                                   int accumulate, cudaStream_t stream) {
+    const long long n_elem = 6 * n_snk;
+    if (n_elem == 0) return cudaSuccess;
+    long long blocks = (n_elem + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    reduce_partials_kernel<<<(unsigned)blocks, 256, 0, stream>>>(partial, n_chunks, n_elem, out, accumulate);
+    return cudaGetLastError();
+}
+
+}  // namespace lyem

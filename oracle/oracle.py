@@ -1,0 +1,219 @@
+"""NumPy front end of the CPU oracle (test infrastructure only).
+
+This module is the checker for the CUDA path: tests, the smoke check and the
+CPU-baseline leg of bench.py use it.  It is never imported by the product
+package.  Visibility is the bit-faithful FP32 restatement in lyem_oracle.c;
+fields are FP64.
+
+Reference behaviour restated here (paths within LyceanEM-Python):
+  - pair visibility + field per (source, sink): lyceanem/src/raycasting_brute_force.cuh:68-88,
+    lyceanem/src/raycasting.cuh:19-95, lyceanem/src/em.cuh:18-120
+  - the self_to_self flag: the C++ parameter `not_self_to_self` receives Python's
+    self_to_self; when it is False the pair whose source index equals its sink
+    index is not tested (lyceanem/src/raycasting_brute_force.cuh:27,
+    lyceanem/models/acceleration_structures.py:99)
+  - one-bounce composition: lyceanem/models/frequency_domain.py:195-264
+  - source sum to sink fields: lyceanem/models/frequency_domain.py:847-849
+  - far-field E_theta/E_phi: lyceanem/models/frequency_domain.py:179-190
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_f32 = ctypes.c_float
+_f64 = ctypes.c_double
+
+EPSILON = np.float32(0.000001)  # lyceanem/src/math_utility.cuh:9
+
+
+def _opt(arr):
+    return None if arr is None else arr.ctypes.data_as(ctypes.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = ctypes.CDLL(path)
+        L.orc_pack_triangles.argtypes = [_f32p, _i64, _i32p, _i64, _f32p]
+        L.orc_mask_brute.argtypes = [_f32p, _i64, _f32p, _i64, _f32p, _i64, _int, _int, _f32, _u8p, _int]
+        L.orc_grid_build.argtypes = [_f32p, _i64, _f64, _f64]
+        L.orc_grid_build.restype = _vp
+        L.orc_grid_free.argtypes = [_vp]
+        L.orc_grid_info.argtypes = [_vp, _f64p, _i32p, _i64p]
+        L.orc_mask_grid.argtypes = [_vp, _f32p, _i64, _f32p, _i64, _int, _int, _f32, _u8p, _int]
+        L.orc_pair_field.argtypes = [_f32p, _f64p, _i64, _f32p, _f32p, _i64, _vp, _f64, _f64, _f64p, _int]
+        L.orc_sink_field.argtypes = [_f32p, _f64p, _vp, _i64, _f32p, _f32p, _i64, _vp, _vp, _vp, _i64,
+                                     _int, _int, _f32, _f64, _f64, _f64p, _i64p, _int]
+        L.orc_rays.argtypes = [_f32p, _i64, _f32p, _i64, _f32p]
+        L.orc_hit_one.argtypes = [_f32p, _f32, _f32p, _f32p, _int, _f32]
+        L.orc_hit_one.restype = _int
+        L.orc_max_threads.restype = _int
+        _lib = L
+    return _lib
+
+
+def _f3(a):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, 3))
+    return a
+
+
+def _c6(E, n):
+    """Complex (n,3) excitation -> float64 (n,6) interleaved (re, im)."""
+    E = np.asarray(E)
+    if E.ndim == 1:
+        E = np.broadcast_to(E.reshape(1, 3), (n, 3))
+    E = np.ascontiguousarray(E.astype(np.complex128).reshape(n, 3))
+    return E.view(np.float64).reshape(n, 6).copy()
+
+
+def max_threads():
+    return int(lib().orc_max_threads())
+
+
+def pack_triangles(verts, idx):
+    """Mesh (V,3) + (T,3) -> (T,12) float32: v0, 0, e1, 0, e2, 0 per triangle."""
+    v = _f3(verts)
+    i = np.ascontiguousarray(np.asarray(idx, dtype=np.int32).reshape(-1, 3))
+    out = np.zeros((i.shape[0], 12), dtype=np.float32)
+    lib().orc_pack_triangles(v, v.shape[0], i, i.shape[0], out)
+    return out
+
+
+def rays(src, snk):
+    s, e = _f3(src), _f3(snk)
+    out = np.zeros((s.shape[0] * e.shape[0], 4), dtype=np.float32)
+    lib().orc_rays(s, s.shape[0], e, e.shape[0], out)
+    return out.reshape(s.shape[0], e.shape[0], 4)
+
+
+def hit_one(d, length, origin, tri12, cull=True, eps=EPSILON):
+    return bool(lib().orc_hit_one(np.ascontiguousarray(d, np.float32), np.float32(length),
+                                  np.ascontiguousarray(origin, np.float32),
+                                  np.ascontiguousarray(tri12, np.float32), int(cull), np.float32(eps)))
+
+
+def mask_brute(src, snk, tris12, self_to_self=False, cull=True, eps=EPSILON, nthreads=0):
+    """Bool (N,M): True where source n sees sink m (brute force over all triangles)."""
+    s, e = _f3(src), _f3(snk)
+    t = np.ascontiguousarray(tris12, dtype=np.float32).reshape(-1, 12)
+    out = np.zeros((s.shape[0], e.shape[0]), dtype=np.uint8)
+    lib().orc_mask_brute(s, s.shape[0], e, e.shape[0], t, t.shape[0], int(not self_to_self),
+                         int(cull), np.float32(eps), out, nthreads)
+    return out.astype(bool)
+
+
+class Grid:
+    """CPU uniform grid over packed triangles (any-hit, FP64 walk, padded boxes)."""
+
+    def __init__(self, tris12, cell, pad=None):
+        self.tris = np.ascontiguousarray(tris12, dtype=np.float32).reshape(-1, 12)
+        pad = 1e-3 * cell if pad is None else pad
+        self.h = lib().orc_grid_build(self.tris, self.tris.shape[0], float(cell), float(pad))
+        oc = np.zeros(4, np.float64)
+        dims = np.zeros(3, np.int32)
+        nref = np.zeros(1, np.int64)
+        lib().orc_grid_info(self.h, oc, dims, nref)
+        self.origin, self.cell, self.dims, self.n_refs = oc[:3], oc[3], dims, int(nref[0])
+
+    def mask(self, src, snk, self_to_self=False, cull=True, eps=EPSILON, nthreads=0):
+        s, e = _f3(src), _f3(snk)
+        out = np.zeros((s.shape[0], e.shape[0]), dtype=np.uint8)
+        lib().orc_mask_grid(self.h, s, s.shape[0], e, e.shape[0], int(not self_to_self), int(cull),
+                            np.float32(eps), out, nthreads)
+        return out.astype(bool)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_grid_free(self.h)
+            self.h = None
+
+
+def pair_field(src, srcE, snk, snk_nrm, mask, alpha, beta, nthreads=0):
+    """FP64 scattering network S[n, m, :] (complex128 (N,M,3)), zero where masked."""
+    s, e, nr = _f3(src), _f3(snk), _f3(snk_nrm)
+    N, M = s.shape[0], e.shape[0]
+    E6 = _c6(srcE, N)
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).reshape(N, M)
+    out = np.zeros((N, M, 6), dtype=np.float64)
+    lib().orc_pair_field(s, E6, N, e, nr, M, _opt(mk), float(alpha), float(beta), out, nthreads)
+    return out.view(np.complex128).reshape(N, M, 3)
+
+
+def sink_field(src, srcE, snk, snk_nrm, alpha, beta, mask=None, grid=None, tris12=None,
+               srcW=None, self_to_self=False, cull=True, eps=EPSILON, nthreads=0,
+               return_counters=False):
+    """FP64 sink field out[m, c] = sum_n w[n, c] S[n, m, c] (complex128 (M,3)).
+
+    Visibility comes from `mask` (bool (N,M)) if given, else it is traced here
+    with `grid` (a Grid) or brute force over `tris12`."""
+    s, e, nr = _f3(src), _f3(snk), _f3(snk_nrm)
+    N, M = s.shape[0], e.shape[0]
+    E6 = _c6(srcE, N)
+    W6 = None if srcW is None else _c6(srcW, N)
+    mk = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8).reshape(N, M)
+    t = None
+    T = 0
+    if mask is None and grid is None:
+        t = np.ascontiguousarray(tris12, dtype=np.float32).reshape(-1, 12)
+        T = t.shape[0]
+    out = np.zeros((M, 6), dtype=np.float64)
+    cnt = np.zeros(2, np.int64)
+    lib().orc_sink_field(s, E6, _opt(W6), N, e, nr, M, _opt(mk), grid.h if grid is not None else None,
+                         _opt(t), T, int(not self_to_self), int(cull), np.float32(eps), float(alpha),
+                         float(beta), out, cnt, nthreads)
+    res = out.view(np.complex128).reshape(M, 3)
+    if return_counters:
+        return res, {"visible": int(cnt[0]), "tests": int(cnt[1])}
+    return res
+
+
+def scattering_network(src, srcE, snk, snk_nrm, tris12, alpha, beta, self_to_self=False,
+                       grid=None, nthreads=0):
+    """The reference's per-pair network (em.calculate_scattering_*): complex128 (N,M,3)."""
+    if grid is not None:
+        mask = grid.mask(src, snk, self_to_self=self_to_self, nthreads=nthreads)
+    else:
+        mask = mask_brute(src, snk, tris12, self_to_self=self_to_self, nthreads=nthreads)
+    return pair_field(src, srcE, snk, snk_nrm, mask, alpha, beta, nthreads=nthreads), mask
+
+
+def onebounce_sink_field(src, srcE, snk, snk_nrm, scat, scat_nrm, alpha, beta, grid=None,
+                         tris12=None, los=True, nthreads=0):
+    """Sink field of calculate_scattering_cuda(scatter_depth=1) summed over sources.
+
+    total = S0 + S1 @ S2 per component with S2 driven by e_p = 1^T S1
+    (frequency_domain.py:230-260), summed over sources (:847-849):
+      E[m, c] = sum_n S0[n,m,c] + sum_p e_p[c] * S2[p,m,c].
+    Returns (E (M,3) complex128, e_p (P,3) complex128)."""
+    kw = dict(grid=grid, tris12=tris12, nthreads=nthreads)
+    N = _f3(src).shape[0]
+    M = _f3(snk).shape[0]
+    direct = sink_field(src, srcE, snk, snk_nrm, alpha, beta, **kw) if los else np.zeros((M, 3), np.complex128)
+    e_p = sink_field(src, srcE, scat, scat_nrm, alpha, beta, **kw)
+    # the scatter points' excitation is stored as complex64 by the reference
+    # (point_data assignment of a complex64 dot product); keep FP64 here.
+    bounce = sink_field(scat, e_p, snk, snk_nrm, alpha, beta, srcW=e_p, **kw)
+    del N
+    return direct + bounce, e_p
+
+
+def farfield_theta_phi(E, theta, phi):
+    """E_theta / E_phi from cartesian E (frequency_domain.py:179-190)."""
+    Ex, Ey, Ez = E[:, 0], E[:, 1], E[:, 2]
+    et = Ex * np.cos(phi) * np.cos(theta) + Ey * np.sin(phi) * np.cos(theta) - Ez * np.sin(theta)
+    ep = -Ex * np.sin(phi) + Ey * np.cos(phi)
+    return et, ep

@@ -1,0 +1,66 @@
+"""The C-ABI library builds, loads without a GPU, and exports every entry point of include/lyem.h."""
+import ctypes
+
+import numpy as np
+
+
+def test_library_exports_header_symbols():
+    from lyceanem_gb300 import build
+    build.build_native()
+    from lyceanem_gb300 import _native
+    names = _native.header_symbols()
+    assert len(names) >= 15
+    lib = _native.load()
+    for n in names:
+        assert hasattr(lib, n), n
+    # every declared entry point has a ctypes signature, and nothing extra is bound
+    assert sorted(_native.SIGNATURES) == names
+
+
+def test_status_strings_and_version():
+    from lyceanem_gb300._native import lib
+    assert lib.lyem_version() >= 100
+    assert lib.lyem_status_string(0) == b"ok"
+    assert lib.lyem_status_string(4) == b"bounded device wait expired"
+    assert lib.lyem_status_string(99) == b"unknown status"
+
+
+def test_grid_plan_host_logic():
+    from lyceanem_gb300._native import lib, f32arr
+    org = (ctypes.c_float * 3)()
+    cell = ctypes.c_float()
+    dims = (ctypes.c_int32 * 3)()
+    b = f32arr([-10, -10, -1, 10, 10, 5])
+    assert lib.lyem_grid_plan(b, 120000, 0.5, org, ctypes.byref(cell), dims) == 0
+    assert cell.value == 0.5
+    assert list(dims) == [41, 41, 13]
+    for k, lo in enumerate([-10, -10, -1]):
+        assert org[k] < lo and org[k] > lo - 0.01
+        assert org[k] + dims[k] * cell.value > [10, 10, 5][k]
+    # automatic cell: about one cell per triangle
+    assert lib.lyem_grid_plan(b, 1000, 0.0, org, ctypes.byref(cell), dims) == 0
+    n = dims[0] * dims[1] * dims[2]
+    assert 500 <= n <= 2000
+    # invalid arguments are reported, not crashed on
+    assert lib.lyem_grid_plan(b, -1, 0.5, org, ctypes.byref(cell), dims) == 1
+    assert lib.lyem_grid_plan(None, 10, 0.5, org, ctypes.byref(cell), dims) == 1
+
+
+def test_workspace_queries():
+    from lyceanem_gb300._native import lib
+    ws = lib.lyem_pair_stage_workspace(1024, 65341, 0, 1, 0)
+    assert ws >= 24 * 65341
+    assert lib.lyem_pair_stage_workspace(64, 2664, 1024, 0, 1) == 64 * 2664 * 24 + 256
+    assert lib.lyem_grid_count_workspace(1000) > 4 * 1000
+    assert lib.lyem_grid_fill_workspace(10000, 100) > 16 * 10000
+
+
+def test_device_entry_points_reject_bad_arguments_without_gpu_work():
+    from lyceanem_gb300._native import lib
+    # negative sizes and null pointers are rejected before any CUDA call
+    assert lib.lyem_pack_triangles(None, 3, None, -1, None, None) == 1
+    assert lib.lyem_pack_triangles(None, 3, None, 0, None, None) == 0
+    assert lib.lyem_mask_to_bytes(None, -1, 3, None, None) == 1
+    assert lib.lyem_em_bin_counts(None, 0, None, 0, 0, 1, 0.0, 1.0, 0.0, None) == 1
+    out = np.zeros(1, np.int32)
+    assert lib.lyem_em_bin_counts(None, 0, None, 0, 1, 1, 0.0, -1.0, 0.0, out.ctypes.data) == 1

@@ -1,0 +1,276 @@
+"""GPU parity: the CUDA path against the CPU oracle on the same seeded inputs.
+
+Masks must be bit-exact; fields within 1e-5 relative (max-normalised) of the
+FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+from helpers import random_scene, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from lyceanem_gb300 import build
+    build.build_native()
+
+
+def _P():
+    from lyceanem_gb300 import propagation as P
+    return P
+
+
+def _no_device_errors():
+    st, flags = _P().device_errors()
+    assert st == 0 and flags == 0, f"device error word {flags:#x}"
+
+
+def _pair_rel(S, So):
+    """per-pair vector error relative to max(|So_pair|, 1e-3 max|So|)."""
+    n = np.linalg.norm(So, axis=-1)
+    e = np.linalg.norm(S - So, axis=-1)
+    return float((e / np.maximum(n, 1e-3 * n.max())).max())
+
+
+def test_direct_config_full_size():
+    """8x8 array, 2,664 sinks, 1,024 triangles, brute force: mask, sink field and per-pair network."""
+    from lyceanem_gb300 import scenes
+    P = _P()
+    s = scenes.direct_scene()
+    beta = 2 * np.pi / s.wavelength
+    tris = P.pack_triangles(torch.from_numpy(s.verts), torch.from_numpy(s.faces))
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    r = P.pair_stage(s.src, s.E, s.snk, s.snk_n, beta=beta, tris=tris, want_mask=True, want_pairs=True, counters=cnt)
+    mask = r.mask().cpu().numpy()
+    _no_device_errors()
+    otris = O.pack_triangles(s.verts, s.faces)
+    assert np.array_equal(tris.cpu().numpy(), otris)
+    omask = O.mask_brute(s.src, s.snk, otris)
+    assert np.array_equal(mask, omask), f"{(mask != omask).sum()} mismatching pairs"
+    ofield = O.sink_field(s.src, s.E, s.snk, s.snk_n, 0.0, beta, mask=omask)
+    assert rel_err(r.sink.cpu().numpy(), ofield) < FIELD_TOL
+    opairs = O.pair_field(s.src, s.E, s.snk, s.snk_n, omask, 0.0, beta)
+    pairs = r.pairs.cpu().numpy()
+    assert np.all(pairs[~omask] == 0)
+    assert _pair_rel(pairs, opairs) < FIELD_TOL
+    assert int(cnt[0]) == int(omask.sum())
+    assert 0 < omask.sum() < omask.size
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_grid_and_brute_masks_bit_exact(seed):
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(seed, n_src=37, n_snk=300, n_tris=700, box=1.0)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    omask = O.mask_brute(src, snk, O.pack_triangles(v, f))
+    rb = P.pair_stage(src, E, snk, snk_n, beta=100.0, tris=tris, want_mask=True)
+    assert np.array_equal(rb.mask().cpu().numpy(), omask)
+    for cell in (None, 0.07, 0.3, 1.9):
+        g = P.UniformGrid(tris, cell=cell)
+        rg = P.pair_stage(src, E, snk, snk_n, beta=100.0, grid=g, want_mask=True)
+        assert np.array_equal(rg.mask().cpu().numpy(), omask), cell
+        assert rel_err(rg.sink.cpu().numpy(), rb.sink.cpu().numpy()) < 1e-6
+    _no_device_errors()
+
+
+def test_grid_build_matches_cpu_binning():
+    """Cell ranges of the device grid equal a NumPy restatement of the padded-box binning."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(3, n_tris=500, box=2.0)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    g = P.UniformGrid(tris, cell=0.4)
+    t = tris.cpu().numpy()
+    vv = np.stack([t[:, 0:3], t[:, 0:3] + t[:, 4:7], t[:, 0:3] + t[:, 8:11]], 1)
+    lo, hi = vv.min(1) - g.cell * 1e-3, vv.max(1) + g.cell * 1e-3
+    org = np.array(g.origin, np.float32)
+    i0 = np.clip(np.floor((lo - org) * np.float32(1 / g.cell)), 0, np.array(g.dims) - 1).astype(int)
+    i1 = np.clip(np.floor((hi - org) * np.float32(1 / g.cell)), 0, np.array(g.dims) - 1).astype(int)
+    cells = [[] for _ in range(g.n_cells)]
+    for k in range(t.shape[0]):
+        for z in range(i0[k, 2], i1[k, 2] + 1):
+            for y in range(i0[k, 1], i1[k, 1] + 1):
+                for x in range(i0[k, 0], i1[k, 0] + 1):
+                    cells[(z * g.dims[1] + y) * g.dims[0] + x].append(k)
+    start = g.cell_start.cpu().numpy()
+    ct = g.cell_tris.cpu().numpy()
+    assert start[-1] == g.n_refs == sum(len(c) for c in cells)
+    for c in range(g.n_cells):
+        got = ct[start[c]:start[c + 1]]
+        assert np.array_equal(got, t[cells[c]]), c
+
+
+def test_bounce_scene_reduced_vs_oracle():
+    """Direct + one bounce (ground + clutter, scatter points) on a reduced bounce recipe."""
+    from lyceanem_gb300 import scenes
+    from lyceanem_gb300.models import acceleration_structures as A
+    from lyceanem_gb300.models.frequency_domain import sink_field
+    P = _P()
+    s = scenes.bounce_scene(n_side=4, n_ground=30, n_clutter=1500, n_scatter=200, el_n=13, az_n=25)
+    beta = 2 * np.pi / s.wavelength
+    dev = A._DeviceScene(s.verts, s.faces, grid_cell=s.cell)
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    E = sink_field(type("S", (), {"device": dev})(), s.src, s.E, s.snk, s.snk_n, 0.0, beta, s.scat, s.scat_n,
+                   scattering=1, counters=cnt).cpu().numpy()
+    _no_device_errors()
+    otris = O.pack_triangles(s.verts, s.faces)
+    og = O.Grid(otris, s.cell)
+    ref, e_p = O.onebounce_sink_field(s.src, s.E, s.snk, s.snk_n, s.scat, s.scat_n, 0.0, beta, grid=og)
+    assert rel_err(E, ref) < FIELD_TOL
+    # stage masks are bit-exact against the oracle
+    for a, an, b, bn in ((s.src, s.src_n, s.snk, s.snk_n), (s.src, s.src_n, s.scat, s.scat_n),
+                         (s.scat, s.scat_n, s.snk, s.snk_n)):
+        r = P.pair_stage(a, np.ones((a.shape[0], 3), np.complex64), b, bn, beta=beta, grid=dev.grid, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), og.mask(a, b))
+
+
+def test_em_dropin_functions():
+    """The four lyceanem.em functions against the oracle network."""
+    from lyceanem_gb300 import em
+    src, snk, snk_n, v, f, E = random_scene(21, n_src=6, n_snk=70, n_tris=130)
+    beta = 2 * np.pi / 0.03
+    normal = np.concatenate([np.tile([[0, 0, 1]], (6, 1)), snk_n]).astype(np.float32)
+    args = (E[:, 0].real, E[:, 0].imag, E[:, 1].real, E[:, 1].imag, E[:, 2].real, E[:, 2].imag, normal)
+    out = em.calculate_scattering_brute_force(src, snk, f, v, 0.03, *args, 0.0, beta, False)
+    S = out.view(np.complex64).reshape(6, 70, 3)
+    So, mask = O.scattering_network(src, E, snk, snk_n, O.pack_triangles(v, f), 0.0, beta)
+    assert np.array_equal(np.any(S != 0, axis=-1), mask & np.any(So != 0, axis=-1))
+    assert _pair_rel(S, So) < FIELD_TOL
+    # tile structure: bins over y-z, then the tiles entry point
+    ymin, zmin, w, ny, nz = -1.4, -1.4, 0.35, 9, 9
+    counts = em.bin_counts_to_numpy(v, f, ny, nz, ymin, w, zmin)
+    assert counts.shape == (ny * nz,) and counts.sum() >= f.shape[0]
+    binned = em.bin_triangles_to_numpy(v, f, ny, nz, ymin, w, zmin, counts, int(counts.sum()))
+    assert binned.shape == (3 * counts.sum(),)
+    assert set(map(tuple, binned.reshape(-1, 3))) == set(map(tuple, f))
+    out2 = em.calculate_scattering_tiles(src, snk, v, 0.03, *args, -2, 2, ymin, 2, zmin, 2, w, counts, binned, ny, nz,
+                                         int(counts.sum()), 0.0, beta, False)
+    S2 = out2.view(np.complex64).reshape(6, 70, 3)
+    assert _pair_rel(S2, So) < FIELD_TOL
+    assert np.array_equal(S2 == 0, S == 0)
+    with pytest.raises(RuntimeError, match="normal.shape"):
+        em.calculate_scattering_brute_force(src, snk, f, v, 0.03, *args[:6], normal[:5], 0.0, beta, False)
+
+
+def test_bins_cover_every_overlapped_cell():
+    from lyceanem_gb300 import em
+    src, snk, snk_n, v, f, E = random_scene(4, n_tris=90, box=1.0)
+    ymin, zmin, w, ny, nz = -1.5, -1.5, 0.25, 12, 12
+    counts = em.bin_counts_to_numpy(v, f, ny, nz, ymin, w, zmin)
+    binned = em.bin_triangles_to_numpy(v, f, ny, nz, ymin, w, zmin, counts, int(counts.sum())).reshape(-1, 3)
+    start = np.concatenate([[0], np.cumsum(counts)])
+    tri = v[f]
+    for k in range(f.shape[0]):
+        lo = tri[k].min(0) - 1e-3 * w
+        hi = tri[k].max(0) + 1e-3 * w
+        iy = np.clip(np.floor((np.array([lo[1], hi[1]]) - ymin) / w), 0, ny - 1).astype(int)
+        iz = np.clip(np.floor((np.array([lo[2], hi[2]]) - zmin) / w), 0, nz - 1).astype(int)
+        for y in range(iy[0], iy[1] + 1):
+            for z in range(iz[0], iz[1] + 1):
+                c = y * nz + z
+                assert any((binned[start[c]:start[c + 1]] == f[k]).all(1)), (k, y, z)
+
+
+def test_numba_engine_visibility_mode():
+    """cull=False, eps=1e-7: the numba engine's rule (rayfunctions.py:37-104)."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(8, n_src=11, n_snk=200, n_tris=300)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f), cull=False, eps=1e-7)
+    r = P.pair_stage(src, E, snk, snk_n, beta=50.0, tris=tris, cull=False, eps=1e-7, want_mask=True)
+    assert np.array_equal(r.mask().cpu().numpy(), om)
+    g = P.UniformGrid(tris, cell=0.2)
+    r2 = P.pair_stage(src, E, snk, snk_n, beta=50.0, grid=g, cull=False, eps=1e-7, want_mask=True)
+    assert np.array_equal(r2.mask().cpu().numpy(), om)
+    assert not np.array_equal(om, O.mask_brute(src, snk, O.pack_triangles(v, f)))
+
+
+def test_self_to_self_flag():
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(13, n_src=40, n_snk=40, n_tris=400, box=0.6)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    ot = O.pack_triangles(v, f)
+    for sts in (False, True):
+        om = O.mask_brute(src, snk, ot, self_to_self=sts)
+        r = P.pair_stage(src, E, snk, snk_n, beta=30.0, tris=tris, self_to_self=sts, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), om)
+        g = P.UniformGrid(tris)
+        r = P.pair_stage(src, E, snk, snk_n, beta=30.0, grid=g, self_to_self=sts, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), om)
+
+
+@pytest.mark.parametrize("n_src,n_snk,n_tris", [(1, 1, 0), (1, 33, 1), (33, 1, 129), (5, 129, 257), (70, 31, 128),
+                                                (3, 200, 1000)])
+def test_edge_sizes(n_src, n_snk, n_tris):
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(n_src * 7 + n_snk, n_src=n_src, n_snk=n_snk, n_tris=max(n_tris, 1))
+    v, f = v[:3 * n_tris], f[:n_tris]
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    ot = O.pack_triangles(v, f)
+    om = O.mask_brute(src, snk, ot)
+    beta = 2 * np.pi / 0.02
+    ref = O.sink_field(src, E, snk, snk_n, 0.0, beta, mask=om)
+    r = P.pair_stage(src, E, snk, snk_n, beta=beta, tris=tris, want_mask=True, want_pairs=True)
+    assert np.array_equal(r.mask().cpu().numpy(), om)
+    assert rel_err(r.sink.cpu().numpy(), ref) < FIELD_TOL
+    if n_tris:
+        g = P.UniformGrid(tris)
+        r = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=g, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), om)
+    _no_device_errors()
+
+
+def test_empty_inputs():
+    P = _P()
+    z = np.zeros((0, 3), np.float32)
+    r = P.pair_stage(z, np.zeros((0, 3), np.complex64), np.ones((4, 3), np.float32), np.ones((4, 3), np.float32),
+                     beta=1.0, tris=None)
+    assert torch.all(r.sink == 0)
+
+
+def test_brute_force_test_counter_without_hits():
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(2, n_src=3, n_snk=50, n_tris=300)
+    v = v + np.float32(100.0)  # move every triangle far away: nothing blocks
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    P.pair_stage(src, E, snk, snk_n, beta=1.0, tris=tris, counters=cnt, self_to_self=True)
+    torch.cuda.synchronize()
+    assert int(cnt[0]) == 150 and int(cnt[1]) == 150 * 300
+
+
+def test_repeatable_bits():
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(6, n_src=64, n_snk=500, n_tris=800)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    g = P.UniformGrid(tris)
+    a = P.pair_stage(src, E, snk, snk_n, beta=300.0, grid=g).sink.clone()
+    b = P.pair_stage(src, E, snk, snk_n, beta=300.0, grid=g).sink.clone()
+    assert torch.equal(a, b)
+
+
+def test_frequency_domain_api():
+    """calculate_scattering (elements False/True) and calculate_farfield through the model API."""
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import frequency_domain as FD
+    src, snk, snk_n, v, f, E = random_scene(17, n_src=5, n_snk=60, n_tris=100)
+    solid = Mesh(v, [("triangle", f)])
+    ap = Mesh(src, point_data={"Normals": np.tile([[0, 0, 1.0]], (5, 1)), "Area": np.full(5, 0.5)})
+    sk = Mesh(snk, point_data={"Normals": snk_n})
+    beta = 2 * np.pi / 0.04
+    axis = np.array([1.0, 0, 0])
+    Ex, Ey, Ez = FD.calculate_scattering(ap, sk, solid, axis, wavelength=0.04, beta=beta, cuda=True)
+    Eo = O.sink_field(src, np.tile(axis * 0.5, (5, 1)), snk, snk_n, 0.0, beta, tris12=O.pack_triangles(v, f))
+    assert rel_err(np.stack([Ex, Ey, Ez], 1), Eo) < FIELD_TOL
+    Sx, Sy, Sz = FD.calculate_scattering(ap, sk, solid, axis, wavelength=0.04, beta=beta, elements=True)
+    assert Sx.shape == (5, 60)
+    assert rel_err(np.stack([Sx, Sy, Sz], -1).sum(0), Eo) < FIELD_TOL
+    et, ep = FD.calculate_farfield(ap, solid, axis, az_range=np.linspace(-180, 180, 9),
+                                   el_range=np.linspace(-90, 90, 5), wavelength=0.04, farfield_distance=5.0, beta=beta)
+    assert et.shape == (45,) and np.isfinite(et).all() and np.isfinite(ep).all()

@@ -1,0 +1,72 @@
+"""Host-side logic on CPU: scene recipes, chunking, steering weights, sink grids."""
+import numpy as np
+
+from lyceanem_gb300 import scenes
+
+
+def test_direct_scene_shapes():
+    s = scenes.direct_scene()
+    assert s.src.shape == (64, 3) and s.snk.shape == (2664, 3) and s.faces.shape == (1024, 3)
+    assert np.allclose(np.linalg.norm(s.snk, axis=1), 10.0, rtol=1e-6)
+    assert np.allclose(s.snk_n, -s.snk / 10.0, atol=1e-6)
+    c = s.verts.reshape(-1, 3, 3).mean(axis=1)
+    assert c[:, :2].min() > -1.06 and c[:, :2].max() < 1.06 and c[:, 2].min() > 0.44 and c[:, 2].max() < 1.56
+    pitch = np.diff(np.unique(s.src[:, 0]))
+    assert np.allclose(pitch, 0.029979 / 2, rtol=1e-5)
+
+
+def test_bounce_scene_shapes():
+    s = scenes.bounce_scene()
+    assert s.src.shape == (1024, 3)
+    assert s.faces.shape == (120000, 3)
+    assert s.scat.shape == (50000, 3)
+    assert s.snk.shape == (65341, 3)
+    assert np.isclose(s.wavelength, 299792458.0 / 28e9)
+    # ground triangles face +z
+    v = s.verts.astype(np.float64)
+    f = s.faces[:80000]
+    n = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    assert (n[:, 2] > 0).all()
+
+
+def test_chunks_follow_reference_loop():
+    from lyceanem_gb300.models.acceleration_structures import _chunks
+    assert _chunks(10, 1) == [(0, 10)]
+    assert _chunks(10, 3) == [(0, 3), (3, 6), (6, 10)]
+    assert _chunks(7, 7) == [(i, i + 1) for i in range(7)]
+
+
+def test_steering_weights_match_far_point_formula():
+    """WavefrontWeights (beamforming.py:81-120): phase k (|p - 1e9 s| - min)."""
+    rng = np.random.default_rng(0)
+    src, _ = scenes.planar_array(8, 8, 0.0107)
+    d = rng.normal(size=(5, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    W = scenes.steering_weights(src, d, 0.0107)
+    for k in range(5):
+        far = d[k] * 1e9
+        dist = np.sqrt(((src.astype(np.float64) - far) ** 2).sum(axis=1))
+        ref = np.exp(1j * 2 * np.pi / 0.0107 * (dist - dist.min()))
+        assert np.abs(W[k] - ref).max() < 2e-3   # the 1e9 far point itself costs ~1e-7 m of path
+    assert np.allclose(np.abs(W), 1.0)
+
+
+def test_spherical_field():
+    from lyceanem_gb300.geometry import spherical_field
+    m = spherical_field(np.linspace(-180, 180, 7), np.linspace(-90, 90, 5), field_radius=3.0)
+    assert m.points.shape == (35, 3)
+    assert np.allclose(np.linalg.norm(m.points, axis=1), 3.0, rtol=1e-6)
+    assert np.allclose(m.point_data["Normals"] * 3.0, -m.points, atol=1e-5)
+    th = m.point_data["theta_(Radians)"]
+    assert np.allclose(np.cos(th) * 3.0, m.points[:, 2], atol=1e-5)
+
+
+def test_sweep_and_batched_recipes_small():
+    s = scenes.sweep_scene(n_side=8, n_clutter=100, n_beams=16, el_n=5, az_n=7, n_ground=10)
+    assert s.weights.shape == (16, 64) and s.faces.shape == (200 + 100, 3)
+    assert (s.directions[:, 2] >= 0).all()
+    sc, snk, snk_n, freqs = scenes.batched_scenes(n_scenes=3, elem_range=(16, 64), tri_range=(1000, 2000),
+                                                  n_sinks=100, n_freqs=4)
+    assert len(sc) == 3 and snk.shape == (100, 3) and freqs.shape == (4,)
+    for s in sc:
+        assert 900 <= s.faces.shape[0] <= 2100
