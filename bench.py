@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Benchmark of the raycasting + frequency-domain propagation path on one GB300.
+
+Workload (default): the direct + one-bounce scene at 28 GHz -- 32x32
+half-wave array, 20x20 m ground plane (80,000 triangles) + 40,000 clutter
+triangles, 50,000 scatter points on triangle centroids, 65,341 far-field sinks
+(1 deg grid at 100 m), uniform grid with 0.5 m cells.  One step = triangle
+packing + grid build + direct stage + source->scatter stage + scatter->sink
+stage (visibility, field, sink sum) with the inputs resident in HBM.
+
+Metric: paths evaluated per second, paths = N*M direct pairs + N*P*M
+source-scatter-sink triples (every path gets mask + field); the visible-path
+count and rate are reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same path (the reference has
+no CPU implementation; its only engines run on the GPU) on the host cores, on a
+bounded sample of the same workload, extrapolated stage by stage.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "lyceanem-python_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "visible paths/s (mask+field) on 1 GB300; mixed-prec vs FP32 sweep at ≤1e-4 rel err"
+OPS_PER_TEST = 30  # FP32-pipe operations of one Moller-Trumbore test (lyceanem/src/raycasting.cuh:23-59)
+L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes per launch of the scatter->sink grid-stage kernel, from the ncu capture summarised in
+# profiles/grid_stage_kernel_bounce.md (None until that capture exists).
+GRID_STAGE_DRAM_BYTES = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["bounce", "direct"], default="bounce")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
+    return ap.parse_args()
+
+
+def workload_scene(name):
+    from lyceanem_gb300 import scenes
+    if name == "direct":
+        return scenes.direct_scene()
+    return scenes.bounce_scene()
+
+
+def describe(s, name):
+    N, M, P, T = s.src.shape[0], s.snk.shape[0], s.scat.shape[0], s.faces.shape[0]
+    paths = N * M + N * P * M
+    if name == "direct":
+        wl = "direct path, 10 GHz, 8x8 array, 2,664 sinks at 10 m, 1,024 obstruction triangles, brute force"
+    else:
+        wl = ("direct + one bounce, 28 GHz, 32x32 array, 80,000 ground + 40,000 clutter triangles, "
+              "50,000 scatter points, 65,341 sinks at 100 m, 0.5 m grid")
+    return {"workload": wl, "n_sources": N, "n_scatter": P, "n_sinks": M, "n_triangles": T, "paths_per_step": paths,
+            "grid_cell_m": s.cell, "l2": "flushed by a 256 MiB device write before every timed step"}, paths
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.gpu_index = gpu_index
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        mhz = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300 import propagation as P
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    s = workload_scene(args.workload)
+    cfg, paths = describe(s, args.workload)
+    beta = 2 * np.pi / s.wavelength
+    t = lambda a, dt=None: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    src, E, snk, snk_n = t(s.src), t(s.E), t(s.snk), t(s.snk_n)
+    scat, scat_n = t(s.scat), t(s.scat_n)
+    verts, faces = t(s.verts), t(s.faces)
+    N, M, Pn = src.shape[0], snk.shape[0], scat.shape[0]
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    cnt_s2 = torch.zeros(2, dtype=torch.int64, device=dev)
+    cnt_all = torch.zeros(2, dtype=torch.int64, device=dev)
+    vis_scat_in = torch.zeros(Pn, dtype=torch.int32, device=dev)
+    vis_scat_out = torch.zeros(Pn, dtype=torch.int32, device=dev)
+    vis_direct = torch.zeros(M, dtype=torch.int32, device=dev)
+    ev = {}
+
+    def step(mark=False):
+        tris = P.pack_triangles(verts, faces)
+        if args.workload == "direct":
+            out = P.pair_stage(src, E, snk, snk_n, beta=beta, tris=tris, counters=cnt_all, snk_visible=vis_direct)
+            if mark:
+                ev["s2"] = (None, None)
+            return out.sink
+        grid = P.UniformGrid(tris, cell=s.cell)
+        out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct).sink
+        e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=cnt_all,
+                           snk_visible=vis_scat_in).sink
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        P.pair_stage(scat, e_p, snk, snk_n, beta=beta, grid=grid, src_W=e_p, sink_out=out, accumulate=True,
+                     counters=cnt_s2, src_visible=vis_scat_out)
+        b.record()
+        if mark:
+            ev.setdefault("s2_list", []).append((a, b))
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # counters describe one step: zero them after warm-up, divide by K afterwards
+    for c in (cnt_s2, cnt_all, vis_scat_in, vis_scat_out, vis_direct):
+        c.zero_()
+    fma_rate = P.fp32_fma_rate()
+    clocks = ClockSampler(dev.index)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = P.kernel_launches()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        step(mark=True)
+        b.record()
+        step_ms.append((a, b))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = P.kernel_launches() - launches0
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in step_ms)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    K = args.steps
+    ms_per_step = total_ms / K
+    value = paths * world * K / (total_ms / 1e3)  # paths per second over all ranks
+    st, flags = P.device_errors()
+    if st != 0 or flags != 0:
+        raise RuntimeError(f"device error word {flags:#x}")
+    vis_direct_total = int(vis_direct.sum().item()) // K
+    if args.workload == "bounce":
+        vin = vis_scat_in.double() / K
+        vout = vis_scat_out.double() / K
+        visible_paths = vis_direct_total + float((vin * vout).sum().item())
+    else:
+        visible_paths = vis_direct_total
+    rays = N * M + (N * Pn + Pn * M if args.workload == "bounce" else 0)
+    res = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+           "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 (visibility bit-specified FP32; field FP32 with FP64 phase)", "data": "synthetic",
+           "config": dict(cfg, parallelism="replicas" if world > 1 else "single GPU"),
+           "visible_paths_per_step": visible_paths, "visible_paths_per_s": visible_paths * world * K / (total_ms / 1e3),
+           "rays_per_s": rays * world * K / (total_ms / 1e3), "gpu_launches": launches}
+    # roofline of the dominant kernel (scatter->sink grid stage; direct stage for the direct workload)
+    if args.workload == "bounce":
+        s2_ms = sum(a.elapsed_time(b) for a, b in ev["s2_list"]) / K
+        tests = int(cnt_s2[1].item()) / K
+        kernel = "grid_stage_kernel (scatter->sink stage incl. its partial-sum reduction)"
+    else:
+        s2_ms = ms_per_step
+        tests = int(cnt_all[1].item()) / K
+        kernel = "brute_stage_kernel (whole step)"
+    achieved = tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12
+    peak = fma_rate / 1e12
+    res["roofline"] = {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                       "frac": achieved / peak, "traffic": GRID_STAGE_DRAM_BYTES,
+                       "peak_source": "measured FP32 FMA lane-op rate (lyem_fp32_fma_probe, same run; FMA = 1 op)",
+                       "tests_per_launch": tests, "ops_per_test": OPS_PER_TEST, "launch_ms": s2_ms,
+                       "share_of_step": s2_ms / ms_per_step}
+    if clk:
+        res["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_e2e:
+        res["e2e"] = run_e2e(args, s, paths)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(args, s, paths)
+    return res
+
+
+def run_e2e(args, s, paths):
+    """Same metric through the reference-shaped host API: numpy in, numpy out, copies inside the timed region."""
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import frequency_domain as FD
+    beta = 2 * np.pi / s.wavelength
+    solid = Mesh(s.verts, [("triangle", s.faces)])
+    ap = Mesh(s.src, point_data={"Normals": s.src_n, "Area": np.ones(s.src.shape[0], np.float32)})
+    sk = Mesh(s.snk, point_data={"Normals": s.snk_n})
+    sc = Mesh(s.scat, point_data={"Normals": s.scat_n}) if s.scat.shape[0] else None
+    scattering = 1 if args.workload == "bounce" else 0
+    axis = np.array([1.0, 0.0, 0.0])
+
+    def call():
+        return FD.calculate_scattering(ap, sk, solid, axis, scatter_points=sc, wavelength=s.wavelength,
+                                       scattering=scattering, beta=beta, cuda=True, grid_cell=s.cell)
+
+    call()
+    torch.cuda.synchronize()
+    K = max(1, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        Ex, Ey, Ez = call()
+    dt = (time.perf_counter() - t0) / K
+    V, T = s.verts.shape[0], s.faces.shape[0]
+    h2d = (3 * (V * 12 + T * 12) + s.src.nbytes + s.src.shape[0] * 24 + s.snk.nbytes + s.snk_n.nbytes
+           + s.scat.nbytes + s.scat_n.nbytes)
+    d2h = Ex.nbytes + Ey.nbytes + Ez.nbytes
+    return {"value": paths / dt, "unit": "paths/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "seconds_per_step": dt,
+            "api": "lyceanem_gb300.models.frequency_domain.calculate_scattering (host numpy in/out, "
+                   "acceleration structure built inside the call)"}
+
+
+# ------------------------------------------------------------------ CPU
+def cpu_sample(s, stride_snk, stride_scat, nthreads):
+    """Times the oracle on every stride-th sink / scatter point; returns per-stage seconds."""
+    import numpy as np
+
+    from oracle import oracle as O
+    beta = 2 * np.pi / s.wavelength
+    snk, snk_n = s.snk[::stride_snk], s.snk_n[::stride_snk]
+    scat, scat_n = s.scat[::stride_scat], s.scat_n[::stride_scat]
+    t0 = time.perf_counter()
+    tris = O.pack_triangles(s.verts, s.faces)
+    grid = O.Grid(tris, s.cell) if s.cell else None
+    kw = dict(grid=grid, tris12=None if grid else tris, nthreads=nthreads)
+    t_build = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.sink_field(s.src, s.E, snk, snk_n, 0.0, beta, **kw)
+    t_direct = time.perf_counter() - t0
+    t_s1 = t_s2 = 0.0
+    if scat.shape[0]:
+        t0 = time.perf_counter()
+        e_p = O.sink_field(s.src, s.E, scat, scat_n, 0.0, beta, **kw)
+        t_s1 = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.sink_field(scat, e_p, snk, snk_n, 0.0, beta, srcW=e_p, **kw)
+        t_s2 = time.perf_counter() - t0
+    return dict(build=t_build, direct=t_direct, s1=t_s1, s2=t_s2, n_snk=snk.shape[0], n_scat=scat.shape[0])
+
+
+def cpu_extrapolate(s, paths, nthreads, target_s):
+    """Calibrate a sample size for ~target_s of CPU work, time it, extrapolate per stage to the full workload."""
+    M, P = s.snk.shape[0], s.scat.shape[0]
+    cal = cpu_sample(s, 256, 256, nthreads)
+    # direct and source->scatter work scale with 1/stride, scatter->sink with 1/stride^2
+    stride = 256
+    while stride > 1:
+        nxt = stride // 2
+        est = (cal["direct"] + cal["s1"]) * (256 / nxt) + cal["s2"] * (256 / nxt) ** 2
+        if est > target_s:
+            break
+        stride = nxt
+    r = cpu_sample(s, stride, stride, nthreads)
+    full = (r["build"] + r["direct"] * M / r["n_snk"]
+            + (r["s1"] * P / r["n_scat"] + r["s2"] * (P * M) / (r["n_scat"] * r["n_snk"]) if r["n_scat"] else 0.0))
+    sample_s = r["build"] + r["direct"] + r["s1"] + r["s2"]
+    desc = (f"oracle (FP32 bit-faithful visibility on a CPU uniform grid, FP64 field) on every {stride}th sink "
+            f"({r['n_snk']}) and scatter point ({r['n_scat']}) with all {s.src.shape[0]} sources; "
+            f"{sample_s:.1f} s measured, extrapolated per stage (direct x M/M', source->scatter x P/P', "
+            f"scatter->sink x PM/(P'M')) to {full:.1f} s for the full step")
+    return paths / full, desc, full
+
+
+def cpu_baseline(args, s, paths):
+    from oracle import oracle as O
+    n = O.max_threads()
+    value, desc, _ = cpu_extrapolate(s, paths, n, args.cpu_seconds)
+    return {"value": value, "unit": "paths/s", "cores": n, "kind": "port", "sample": desc}
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the path on the host cores (the reference has no CPU engine)."""
+    from oracle import oracle as O
+    s = workload_scene(args.workload)
+    cfg, paths = describe(s, args.workload)
+    n = O.max_threads()
+    vals, descs, fulls = [], [], []
+    for _ in range(max(1, args.steps)):
+        v, d, full = cpu_extrapolate(s, paths, n, args.cpu_seconds / max(1, args.steps))
+        vals.append(v)
+        descs.append(d)
+        fulls.append(full)
+    value = len(vals) / sum(1.0 / v for v in vals)
+    ms = 1e3 * sum(fulls) / len(fulls)
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 visibility / f64 field (CPU)", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": n, "kind": "port", "sample": descs[-1]},
+            "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, rank, world)), flush=True)
+        return 0
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

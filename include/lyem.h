@@ -53,6 +53,13 @@ LYEM_API int lyem_version(void);
 LYEM_API const char *lyem_status_string(int status);
 /* cudaError_t of the last failing CUDA call made by this library (0 if none). */
 LYEM_API int lyem_last_cuda_error(void);
+/* Number of kernels this library has launched in this process so far (all
+ * entry points, all threads); the difference across a region counts its launches. */
+LYEM_API uint64_t lyem_kernel_launches(void);
+/* Calibration probe with no counterpart in the reference: runs a dependent-FMA
+ * loop on every SM (iterations per thread, >= 16) and reports the achieved FP32
+ * FMA lane-operations per second, the denominator of the visibility roofline. */
+LYEM_API int lyem_fp32_fma_probe(int64_t iterations, double *fma_per_second, void *stream);
 /* Synchronises `stream`, then reads and clears the library's device error word
  * (bit 0: a bounded wait expired; bit 1: an index check failed).  Returns
  * LYEM_ERR_TIMEOUT if bit 0 was set. */
@@ -120,7 +127,9 @@ LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *or
  * Optional outputs (NULL to skip): d_pair_out [n_src, n_snk, 6] (the
  * reference's scattering network layout, zero for blocked pairs), d_mask_bits
  * [n_src, ceil(n_snk/32)] uint32 (bit m%32 of word m/32 = visible),
- * d_counters uint64[2] incremented by (visible pairs, ray/triangle tests).
+ * d_counters uint64[2] incremented by (visible pairs, ray/triangle tests),
+ * d_src_visible int32[n_src] / d_snk_visible int32[n_snk] incremented by the
+ * visible pairs of each source / sink.
  * src_chunk: sources per thread block (0 = automatic). */
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
                                           int32_t src_chunk);
@@ -130,7 +139,8 @@ LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const
                              const float *grid_origin3, float grid_cell, const int32_t *grid_dims3, double alpha,
                              double beta, int32_t self_to_self, int32_t cull, float eps, float *d_sink_out,
                              int32_t accumulate, float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
-                             int32_t src_chunk, void *d_ws, size_t ws_bytes, void *stream);
+                             int32_t *d_src_visible, int32_t *d_snk_visible, int32_t src_chunk, void *d_ws,
+                             size_t ws_bytes, void *stream);
 
 /* Expands a bit mask [n_src, ceil(n_snk/32)] to bytes [n_src, n_snk] (0/1). */
 LYEM_API int lyem_mask_to_bytes(const uint32_t *d_mask_bits, int64_t n_src, int64_t n_snk, uint8_t *d_out,

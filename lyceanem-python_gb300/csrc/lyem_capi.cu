@@ -143,6 +143,14 @@ LYEM_API const char* lyem_status_string(int status) {
 
 LYEM_API int lyem_last_cuda_error(void) { return g_last_cuda_error; }
 
+LYEM_API uint64_t lyem_kernel_launches(void) { return (uint64_t)launches_so_far(); }
+
+LYEM_API int lyem_fp32_fma_probe(int64_t iterations, double* fma_per_second, void* stream) {
+    if (iterations < 16 || !fma_per_second) return LYEM_ERR_INVALID;
+    LYEM_CK(fma_probe(iterations, fma_per_second, as_stream(stream)));
+    return LYEM_OK;
+}
+
 LYEM_API int lyem_device_errors(void* stream, uint32_t* flags_out) {
     unsigned int flags = 0;
     LYEM_CK(read_clear_device_errors(&flags, as_stream(stream)));
@@ -156,7 +164,7 @@ LYEM_API int lyem_pack_triangles(const float* d_verts, int64_t n_verts, const in
     if (n_tris == 0) return LYEM_OK;
     if (!d_verts || !d_idx || !d_tris || !aligned16(d_tris)) return LYEM_ERR_INVALID;
     pack_triangles_kernel<<<blocks_for(n_tris, 256), 256, 0, as_stream(stream)>>>(
-        d_verts, n_verts, d_idx, n_tris, reinterpret_cast<float4*>(d_tris), device_error_word());
+        d_verts, n_verts, d_idx, n_tris, reinterpret_cast<float4*>(d_tris), device_error_word()); note_launches(1);
     LYEM_CK(cudaGetLastError());
     return LYEM_OK;
 }
@@ -263,7 +271,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
                              const float* grid_origin3, float grid_cell, const int32_t* grid_dims3, double alpha,
                              double beta, int32_t self_to_self, int32_t cull, float eps, float* d_sink_out,
                              int32_t accumulate, float* d_pair_out, uint32_t* d_mask_bits, uint64_t* d_counters,
-                             int32_t src_chunk, void* d_ws, size_t ws_bytes, void* stream) {
+                             int32_t* d_src_visible, int32_t* d_snk_visible, int32_t src_chunk, void* d_ws,
+                             size_t ws_bytes, void* stream) {
     if (n_src < 0 || n_snk < 0 || n_tris < 0) return LYEM_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
     const bool use_grid = d_cell_start != nullptr;
@@ -321,6 +330,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     p.mask_bits = d_mask_bits;
     p.mask_words = (n_snk + 31) / 32;
     p.counters = reinterpret_cast<unsigned long long*>(d_counters);
+    p.src_visible = d_src_visible;
+    p.snk_visible = d_snk_visible;
     LYEM_CK(launch_pair_stage(p, cull, s));
     if (d_sink_out) {
         const long long chunks = (n_src + chunk - 1) / chunk;
@@ -335,7 +346,7 @@ LYEM_API int lyem_mask_to_bytes(const uint32_t* d_mask_bits, int64_t n_src, int6
     if (n_src * n_snk == 0) return LYEM_OK;
     if (!d_mask_bits || !d_out) return LYEM_ERR_INVALID;
     mask_to_bytes_kernel<<<blocks_for(n_src * n_snk, 256), 256, 0, as_stream(stream)>>>(
-        d_mask_bits, n_src, n_snk, (n_snk + 31) / 32, d_out);
+        d_mask_bits, n_src, n_snk, (n_snk + 31) / 32, d_out); note_launches(1);
     LYEM_CK(cudaGetLastError());
     return LYEM_OK;
 }
@@ -387,7 +398,7 @@ int em_bin_common(const float* tri_vertex, int64_t n_vertex, const int32_t* tri_
     LYEM_CK(dt.alloc(48 * (size_t)n_tris, s));
     if (n_tris > 0) {
         pack_triangles_kernel<<<blocks_for(n_tris, 256), 256, 0, s>>>(dv.as<float>(), n_vertex, di.as<int>(), n_tris,
-                                                                     dt.as<float4>(), device_error_word());
+                                                                     dt.as<float4>(), device_error_word()); note_launches(1);
         LYEM_CK(cudaGetLastError());
     }
     BinSpec b = yz_spec(ncells_x, ncells_y, ymin, cell_width, z_min);
@@ -452,7 +463,7 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
     LYEM_CK(dt.alloc(48 * (size_t)n_tris, s));
     if (n_tris > 0) {
         pack_triangles_kernel<<<blocks_for(n_tris, 256), 256, 0, s>>>(dv.as<float>(), n_vertex, di.as<int>(), n_tris,
-                                                                     dt.as<float4>(), device_error_word());
+                                                                     dt.as<float4>(), device_error_word()); note_launches(1);
         LYEM_CK(cudaGetLastError());
     }
     const size_t pair_bytes = 24 * (size_t)n_source * (size_t)n_end;
@@ -493,8 +504,8 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
     int st = lyem_pair_stage(dsrc.as<float>(), dE.as<float>(), nullptr, n_source, dend.as<float>(), dnrm.as<float>(),
                              n_end, dt.as<float>(), n_tris, grid_on ? dstart.as<int32_t>() : nullptr,
                              grid_on ? dcell.as<float>() : nullptr, org, cell, dims, (double)alpha, (double)beta,
-                             not_self_to_self, 1, kEpsilon, nullptr, 0, dpair.as<float>(), nullptr, nullptr, 0, dws.p,
-                             ws, s);
+                             not_self_to_self, 1, kEpsilon, nullptr, 0, dpair.as<float>(), nullptr, nullptr, nullptr,
+                             nullptr, 0, dws.p, ws, s);
     if (st != LYEM_OK) return st;
     LYEM_CK(cudaMemcpyAsync(out, dpair.p, pair_bytes, cudaMemcpyDeviceToHost, s));
     LYEM_CK(cudaStreamSynchronize(s));

@@ -83,11 +83,11 @@ __global__ void bounds_decode_kernel(float* bounds6) {
 }
 
 cudaError_t launch_tris_bounds(const float4* tris, long long n_tris, float* bounds6, cudaStream_t stream) {
-    bounds_init_kernel<<<1, 32, 0, stream>>>(bounds6);
+    bounds_init_kernel<<<1, 32, 0, stream>>>(bounds6); note_launches(1);
     long long blocks = (n_tris + 255) / 256;
     blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
-    tris_bounds_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tris, n_tris, bounds6);
-    bounds_decode_kernel<<<1, 32, 0, stream>>>(bounds6);
+    tris_bounds_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tris, n_tris, bounds6); note_launches(1);
+    bounds_decode_kernel<<<1, 32, 0, stream>>>(bounds6); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -213,16 +213,16 @@ cudaError_t exclusive_scan(const int* in, int* out, long long n, int* ws, cudaSt
     if (n <= 0) return cudaSuccess;
     long long nb = (n + kScanBlock - 1) / kScanBlock;
     if (nb == 1) {
-        scan_block_kernel<<<1, 256, 0, stream>>>(in, out, n, nullptr);
+        scan_block_kernel<<<1, 256, 0, stream>>>(in, out, n, nullptr); note_launches(1);
         return cudaGetLastError();
     }
     int* sums = ws;
     int* sums_scanned = ws + nb + 32;
     int* rest = sums_scanned + nb + 32;
-    scan_block_kernel<<<(unsigned)nb, 256, 0, stream>>>(in, out, n, sums);
+    scan_block_kernel<<<(unsigned)nb, 256, 0, stream>>>(in, out, n, sums); note_launches(1);
     cudaError_t e = exclusive_scan(sums, sums_scanned, nb, rest, stream);
     if (e != cudaSuccess) return e;
-    add_block_offsets_kernel<<<(unsigned)nb, 256, 0, stream>>>(out, n, sums_scanned);
+    add_block_offsets_kernel<<<(unsigned)nb, 256, 0, stream>>>(out, n, sums_scanned); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -292,10 +292,10 @@ cudaError_t radix_sort_pairs(int* k0, int* v0, int* k1, int* v1, long long n, in
     const int nblocks = (int)((n + kSortTile - 1) / kSortTile);
     int *ki = k0, *vi = v0, *ko = k1, *vo = v1;
     for (int p = 0; p < passes; ++p) {
-        radix_hist_kernel<<<nblocks, kSortThreads, 0, stream>>>(ki, n, 8 * p, hist, nblocks);
+        radix_hist_kernel<<<nblocks, kSortThreads, 0, stream>>>(ki, n, 8 * p, hist, nblocks); note_launches(1);
         cudaError_t e = exclusive_scan(hist, hist_scanned, 256LL * nblocks, scan_ws, stream);
         if (e != cudaSuccess) return e;
-        radix_scatter_kernel<<<nblocks, kSortThreads, 0, stream>>>(ki, vi, ko, vo, n, 8 * p, hist_scanned, nblocks);
+        radix_scatter_kernel<<<nblocks, kSortThreads, 0, stream>>>(ki, vi, ko, vo, n, 8 * p, hist_scanned, nblocks); note_launches(1);
         std::swap(ki, ko);
         std::swap(vi, vo);
     }
@@ -356,7 +356,7 @@ cudaError_t grid_count(const BinSpec& b, const float4* tris, long long n_tris, i
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counts + n_tris, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
-    if (n_tris > 0) count_refs_kernel<<<grid_blocks(n_tris, 256), 256, 0, stream>>>(b, tris, n_tris, counts, total);
+    if (n_tris > 0) { count_refs_kernel<<<grid_blocks(n_tris, 256), 256, 0, stream>>>(b, tris, n_tris, counts, total); note_launches(1); }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return exclusive_scan(counts, tri_offsets, n_tris + 1, scan_ws, stream);
@@ -381,7 +381,7 @@ cudaError_t grid_sort(const BinSpec& b, const float4* tris, long long n_tris, co
     int* hist_scanned = hist + 256 * nblocks + 64;
     int* scan_ws = hist_scanned + 256 * nblocks + 64;
     const long long ncells = (long long)b.dims[0] * b.dims[1] * b.dims[2];
-    if (n_refs > 0) emit_refs_kernel<<<grid_blocks(n_tris, 256), 256, 0, stream>>>(b, tris, n_tris, tri_offsets, k0, v0);
+    if (n_refs > 0) { emit_refs_kernel<<<grid_blocks(n_tris, 256), 256, 0, stream>>>(b, tris, n_tris, tri_offsets, k0, v0); note_launches(1); }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     bool first = true;
@@ -391,7 +391,7 @@ cudaError_t grid_sort(const BinSpec& b, const float4* tris, long long n_tris, co
     }
     const int* keys = first ? k0 : k1;
     *vals_out = first ? v0 : v1;
-    cell_start_kernel<<<grid_blocks(ncells + 1, 256), 256, 0, stream>>>(keys, n_refs, ncells, cell_start);
+    cell_start_kernel<<<grid_blocks(ncells + 1, 256), 256, 0, stream>>>(keys, n_refs, ncells, cell_start); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -400,7 +400,7 @@ cudaError_t grid_fill(const BinSpec& b, const float4* tris, long long n_tris, co
     const int* vals = nullptr;
     cudaError_t e = grid_sort(b, tris, n_tris, tri_offsets, n_refs, cell_start, &vals, ws, stream);
     if (e != cudaSuccess) return e;
-    if (n_refs > 0) gather_tris_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tris, vals, n_refs, cell_tris);
+    if (n_refs > 0) { gather_tris_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tris, vals, n_refs, cell_tris); note_launches(1); }
     return cudaGetLastError();
 }
 
@@ -411,7 +411,7 @@ cudaError_t bin_fill_index(const BinSpec& b, const float4* tris, long long n_tri
     cudaError_t e = grid_sort(b, tris, n_tris, tri_offsets, n_refs, cell_start, &vals, ws, stream);
     if (e != cudaSuccess) return e;
     if (n_refs > 0)
-        gather_index_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tri_index, vals, n_refs, out_index);
+        gather_index_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tri_index, vals, n_refs, out_index); note_launches(1);
     return cudaGetLastError();
 }
 

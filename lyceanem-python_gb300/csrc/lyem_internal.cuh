@@ -52,7 +52,16 @@ struct StageParams {
     unsigned int* mask_bits;     // [n_src, mask_words] or nullptr
     long long mask_words;
     unsigned long long* counters;  // [0] visible pairs, [1] ray/triangle tests (may be nullptr)
+    int* src_visible;              // [n_src] visible sinks per source (may be nullptr)
+    int* snk_visible;              // [n_snk] visible sources per sink (may be nullptr)
 };
+
+// Host-side count of kernel launches made by this library (lyem_kernel_launches()).
+void note_launches(unsigned long long n);
+unsigned long long launches_so_far();
+
+// FP32 FMA lane-operations per second of this device (calibration probe).
+cudaError_t fma_probe(long long iters, double* fma_per_s, cudaStream_t stream);
 
 // Host-side launchers (lyem_stage.cu).
 cudaError_t launch_pair_stage(const StageParams& p, int cull, cudaStream_t stream);

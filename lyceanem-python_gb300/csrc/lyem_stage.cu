@@ -25,12 +25,59 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "lyem_device.cuh"
 #include "lyem_internal.cuh"
 
 namespace lyem {
 
 __device__ unsigned int g_device_error = 0;
+
+static std::atomic<unsigned long long> g_launches{0};
+void note_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+unsigned long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void fma_probe_kernel(long long iters, float seed, float* sink) {
+    float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+    float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+    const float b = 0.999999f, c = 1e-7f;
+    for (long long i = 0; i < iters; ++i) {
+        a0 = __fmaf_rn(a0, b, c); a1 = __fmaf_rn(a1, b, c); a2 = __fmaf_rn(a2, b, c); a3 = __fmaf_rn(a3, b, c);
+        a4 = __fmaf_rn(a4, b, c); a5 = __fmaf_rn(a5, b, c); a6 = __fmaf_rn(a6, b, c); a7 = __fmaf_rn(a7, b, c);
+    }
+    float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.f) sink[0] = s;  // keeps the chains alive
+}
+
+cudaError_t fma_probe(long long iters, double* fma_per_s, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    float* sink = nullptr;
+    e = cudaMallocAsync(&sink, 16, stream);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 8, threads = 256;
+    fma_probe_kernel<<<blocks, threads, 0, stream>>>(iters / 4, 1.f, sink); note_launches(1);
+    cudaEventRecord(a, stream);
+    fma_probe_kernel<<<blocks, threads, 0, stream>>>(iters, 1.f, sink); note_launches(1);
+    cudaEventRecord(b, stream);
+    e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFreeAsync(sink, stream);
+    if (e != cudaSuccess) return e;
+    *fma_per_s = (double)blocks * threads * 8.0 * (double)iters / (ms * 1e-3);
+    return cudaGetLastError();
+}
 
 unsigned int* device_error_word() {
     void* p = nullptr;
@@ -102,10 +149,16 @@ __device__ __forceinline__ void pair_epilogue(const StageParams& p, long long n,
     }
 }
 
-__device__ __forceinline__ void write_mask(const StageParams& p, long long n, long long m, bool vis) {
+// Mask bits of the warp's 32 sinks for source n, and the per-source visible count.
+template <bool MASK_OUT>
+__device__ __forceinline__ void record_visibility(const StageParams& p, long long n, long long m, bool vis) {
+    if (!MASK_OUT && !p.src_visible) return;
     unsigned b = __ballot_sync(0xffffffffu, vis);
-    long long w = m >> 5;
-    if ((threadIdx.x & 31) == 0 && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
+    if ((threadIdx.x & 31) == 0) {
+        long long w = m >> 5;
+        if (MASK_OUT && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
+        if (p.src_visible && b) atomicAdd(p.src_visible + n, __popc(b));
+    }
 }
 
 __device__ __forceinline__ void flush_block(const StageParams& p, long long m, bool m_ok, const float* acc,
@@ -115,6 +168,7 @@ __device__ __forceinline__ void flush_block(const StageParams& p, long long m, b
         dst[0] = make_float2(acc[0], acc[1]);
         dst[1] = make_float2(acc[2], acc[3]);
         dst[2] = make_float2(acc[4], acc[5]);
+        if (p.snk_visible && vis_count) atomicAdd(p.snk_visible + m, (int)vis_count);
     }
     if (p.counters) {
 #pragma unroll
@@ -224,7 +278,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     for (int s = 0; s < nsrc; ++s) {
         const long long n = n0 + s;
         const bool vis = m_ok && !((blocked >> s) & 1u);
-        if (MASK_OUT) write_mask(p, n, m, vis);
+        record_visibility<MASK_OUT>(p, n, m, vis);
         const float* so = p.src_pos + 3 * n;
         pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;
@@ -323,7 +377,7 @@ __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams 
             const Ray r = make_ray(ox, oy, oz, ex, ey, ez);
             vis = !grid_blocked<CULL>(p, ox, oy, oz, r, tests);
         }
-        if (MASK_OUT) write_mask(p, n, m, vis);
+        record_visibility<MASK_OUT>(p, n, m, vis);
         pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, ox, oy, oz, ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;
     }
@@ -345,13 +399,13 @@ static cudaError_t launch_t(const StageParams& p, cudaStream_t stream) {
     const long long chunks = (p.n_src + p.src_chunk - 1) / p.src_chunk;
     dim3 grid((unsigned)((p.n_snk + kThreads - 1) / kThreads), (unsigned)chunks);
     if (p.cell_start) {
-        grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT><<<grid, kThreads, 0, stream>>>(p);
+        grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT><<<grid, kThreads, 0, stream>>>(p); note_launches(1);
     } else {
         const size_t smem = sizeof(BruteSmem);
         auto kern = brute_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        kern<<<grid, kThreads, smem, stream>>>(p);
+        kern<<<grid, kThreads, smem, stream>>>(p); note_launches(1);
     }
     return cudaGetLastError();
 }
@@ -380,7 +434,7 @@ cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, lon
     if (n_elem == 0) return cudaSuccess;
     long long blocks = (n_elem + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    reduce_partials_kernel<<<(unsigned)blocks, 256, 0, stream>>>(partial, n_chunks, n_elem, out, accumulate);
+    reduce_partials_kernel<<<(unsigned)blocks, 256, 0, stream>>>(partial, n_chunks, n_elem, out, accumulate); note_launches(1);
     return cudaGetLastError();
 }
 

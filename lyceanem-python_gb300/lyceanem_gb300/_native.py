@@ -48,6 +48,8 @@ SIGNATURES = {
     "lyem_version": ([], ctypes.c_int),
     "lyem_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "lyem_last_cuda_error": ([], ctypes.c_int),
+    "lyem_kernel_launches": ([], ctypes.c_uint64),
+    "lyem_fp32_fma_probe": ([_i64, ctypes.POINTER(ctypes.c_double), _vp], ctypes.c_int),
     "lyem_device_errors": ([_vp, _u32p], ctypes.c_int),
     "lyem_pack_triangles": ([_vp, _i64, _vp, _i64, _vp, _vp], ctypes.c_int),
     "lyem_tris_bounds": ([_vp, _i64, _vp, _vp], ctypes.c_int),
@@ -58,7 +60,7 @@ SIGNATURES = {
     "lyem_grid_fill": ([_vp, _i64, _f32p, _f32, _i32p, _vp, _i64, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_pair_stage_workspace": ([_i64, _i64, _i64, _i32, _i32], _sz),
     "lyem_pair_stage": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _f32p, _f32, _i32p, _f64, _f64,
-                         _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _i32, _vp, _sz, _vp], ctypes.c_int),
+                         _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _i32, _vp, _sz, _vp], ctypes.c_int),
     "lyem_mask_to_bytes": ([_vp, _i64, _i64, _vp, _vp], ctypes.c_int),
     "lyem_em_bin_counts": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp], ctypes.c_int),
     "lyem_em_bin_triangles": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp, _i64, _vp], ctypes.c_int),

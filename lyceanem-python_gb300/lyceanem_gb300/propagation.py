@@ -131,13 +131,16 @@ class StageResult:
 
 def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, grid=None, src_W=None,
                self_to_self=False, cull=True, eps=EPSILON, sink_out=None, accumulate=False, want_pairs=False,
-               want_mask=False, counters=None, src_chunk=0, workspace=None):
+               want_mask=False, counters=None, src_visible=None, snk_visible=None, src_chunk=0, workspace=None):
     """Visibility + fused field of every (source, sink) pair.
 
     Returns a StageResult whose .sink is complex64 [n_snk,3] with
         sink[m, c] (+)= sum_n W[n, c] * S[n, m, c]
     (W = src_W or 1), .pairs the per-pair network complex64 [n_src,n_snk,3]
     when want_pairs, and .mask_bits the visibility bit mask when want_mask.
+    counters (int64 [2]) accumulates (visible pairs, ray/triangle tests);
+    src_visible / snk_visible (int32 [n_src] / [n_snk]) accumulate visible pairs
+    per source / per sink.
     Visibility uses `grid` (a UniformGrid) if given, else brute force over
     `tris`.  self_to_self=False reproduces the reference's untested pair
     n == m (lyceanem/src/raycasting_brute_force.cuh:27)."""
@@ -172,7 +175,8 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
                              float(beta), int(bool(self_to_self)), int(bool(cull)), float(eps),
                              _p(torch.view_as_real(sink_out)), int(bool(accumulate)),
                              _p(None if pairs is None else torch.view_as_real(pairs)), _p(mbits), _p(counters),
-                             int(src_chunk), _p(workspace), workspace.numel(), _stream())
+                             _p(src_visible), _p(snk_visible), int(src_chunk), _p(workspace), workspace.numel(),
+                             _stream())
     check(st, "pair_stage")
     return StageResult(sink_out, pairs, mbits, counters, N, M)
 
@@ -182,6 +186,18 @@ def device_errors():
     flags = ctypes.c_uint32()
     st = lib.lyem_device_errors(_stream(), ctypes.byref(flags))
     return st, flags.value
+
+
+def kernel_launches():
+    """Cumulative number of kernels launched by liblyem_gpu.so in this process."""
+    return int(lib.lyem_kernel_launches())
+
+
+def fp32_fma_rate(iterations=1 << 16):
+    """Measured FP32 FMA lane-operations per second of the current device."""
+    out = ctypes.c_double()
+    check(lib.lyem_fp32_fma_probe(int(iterations), ctypes.byref(out), _stream()), "fp32_fma_probe")
+    return out.value
 
 
 def wavenumber(wavelength):

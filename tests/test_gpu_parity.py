@@ -32,11 +32,20 @@ def _no_device_errors():
     assert st == 0 and flags == 0, f"device error word {flags:#x}"
 
 
-def _pair_rel(S, So):
-    """per-pair vector error relative to max(|So_pair|, 1e-3 max|So|)."""
-    n = np.linalg.norm(So, axis=-1)
+def _pair_rel(S, So, src=None, snk=None, E=None, beta=None, alpha=0.0):
+    """Per-pair vector error relative to the pair's unprojected amplitude
+    |E_n| |alpha + 1/r + j beta| exp(-alpha r) / (2 pi r): the polarisation
+    projection and n.d can make a pair's field arbitrarily small, while the FP32
+    ray direction carries an absolute error of ~1e-7 of that amplitude.  Without
+    geometry the scale falls back to the largest pair."""
     e = np.linalg.norm(S - So, axis=-1)
-    return float((e / np.maximum(n, 1e-3 * n.max())).max())
+    if src is None:
+        n = np.linalg.norm(So, axis=-1)
+        return float((e / n.max()).max())
+    r = np.linalg.norm(snk[None].astype(np.float64) - src[:, None].astype(np.float64), axis=-1)
+    amp = np.linalg.norm(np.asarray(E, np.complex128), axis=-1)[:, None]
+    scale = amp * np.abs(alpha + 1.0 / r + 1j * beta) * np.exp(-alpha * r) / (2 * np.pi * r)
+    return float((e / np.maximum(scale, 1e-30)).max())
 
 
 def test_direct_config_full_size():
@@ -59,7 +68,7 @@ def test_direct_config_full_size():
     opairs = O.pair_field(s.src, s.E, s.snk, s.snk_n, omask, 0.0, beta)
     pairs = r.pairs.cpu().numpy()
     assert np.all(pairs[~omask] == 0)
-    assert _pair_rel(pairs, opairs) < FIELD_TOL
+    assert _pair_rel(pairs, opairs, s.src, s.snk, s.E, beta) < FIELD_TOL
     assert int(cnt[0]) == int(omask.sum())
     assert 0 < omask.sum() < omask.size
 
@@ -134,14 +143,14 @@ def test_em_dropin_functions():
     """The four lyceanem.em functions against the oracle network."""
     from lyceanem_gb300 import em
     src, snk, snk_n, v, f, E = random_scene(21, n_src=6, n_snk=70, n_tris=130)
-    beta = 2 * np.pi / 0.03
+    beta = float(np.float32(2 * np.pi / 0.03))  # the em interface takes beta as float32
     normal = np.concatenate([np.tile([[0, 0, 1]], (6, 1)), snk_n]).astype(np.float32)
     args = (E[:, 0].real, E[:, 0].imag, E[:, 1].real, E[:, 1].imag, E[:, 2].real, E[:, 2].imag, normal)
     out = em.calculate_scattering_brute_force(src, snk, f, v, 0.03, *args, 0.0, beta, False)
     S = out.view(np.complex64).reshape(6, 70, 3)
     So, mask = O.scattering_network(src, E, snk, snk_n, O.pack_triangles(v, f), 0.0, beta)
     assert np.array_equal(np.any(S != 0, axis=-1), mask & np.any(So != 0, axis=-1))
-    assert _pair_rel(S, So) < FIELD_TOL
+    assert _pair_rel(S, So, src, snk, E, beta) < FIELD_TOL
     # tile structure: bins over y-z, then the tiles entry point
     ymin, zmin, w, ny, nz = -1.4, -1.4, 0.35, 9, 9
     counts = em.bin_counts_to_numpy(v, f, ny, nz, ymin, w, zmin)
@@ -152,7 +161,7 @@ def test_em_dropin_functions():
     out2 = em.calculate_scattering_tiles(src, snk, v, 0.03, *args, -2, 2, ymin, 2, zmin, 2, w, counts, binned, ny, nz,
                                          int(counts.sum()), 0.0, beta, False)
     S2 = out2.view(np.complex64).reshape(6, 70, 3)
-    assert _pair_rel(S2, So) < FIELD_TOL
+    assert _pair_rel(S2, So, src, snk, E, beta) < FIELD_TOL
     assert np.array_equal(S2 == 0, S == 0)
     with pytest.raises(RuntimeError, match="normal.shape"):
         em.calculate_scattering_brute_force(src, snk, f, v, 0.03, *args[:6], normal[:5], 0.0, beta, False)
