@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["bounce", "direct"], default="bounce")
+    ap.add_argument("--workload", choices=["bounce", "direct", "bounce_small"], default="bounce",
+                    help="bounce_small: the bounce scene with 2,000 scatter points and a 4 deg sink grid "
+                         "(profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
@@ -56,6 +58,8 @@ def workload_scene(name):
     from lyceanem_gb300 import scenes
     if name == "direct":
         return scenes.direct_scene()
+    if name == "bounce_small":
+        return scenes.bounce_scene(n_scatter=2000, el_n=46, az_n=91)
     return scenes.bounce_scene()
 
 
@@ -64,6 +68,9 @@ def describe(s, name):
     paths = N * M + N * P * M
     if name == "direct":
         wl = "direct path, 10 GHz, 8x8 array, 2,664 sinks at 10 m, 1,024 obstruction triangles, brute force"
+    elif name == "bounce_small":
+        wl = ("profiling case: bounce scene with 2,000 scatter points and 4,186 sinks (4 deg grid at 100 m), "
+              "0.5 m grid")
     else:
         wl = ("direct + one bounce, 28 GHz, 32x32 array, 80,000 ground + 40,000 clutter triangles, "
               "50,000 scatter points, 65,341 sinks at 100 m, 0.5 m grid")
@@ -149,14 +156,15 @@ def run_ours(args, rank, world):
                 ev["s2"] = (None, None)
             return out.sink
         grid = P.UniformGrid(tris, cell=s.cell)
+        o_scat = P.spatial_order(scat)  # scatter points are traced in Morton order
         out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct).sink
         e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=cnt_all,
-                           snk_visible=vis_scat_in).sink
+                           snk_visible=vis_scat_in, snk_order=o_scat).sink
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
         P.pair_stage(scat, e_p, snk, snk_n, beta=beta, grid=grid, src_W=e_p, sink_out=out, accumulate=True,
-                     counters=cnt_s2, src_visible=vis_scat_out)
+                     counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat)
         b.record()
         if mark:
             ev.setdefault("s2_list", []).append((a, b))
@@ -201,13 +209,13 @@ def run_ours(args, rank, world):
     if st != 0 or flags != 0:
         raise RuntimeError(f"device error word {flags:#x}")
     vis_direct_total = int(vis_direct.sum().item()) // K
-    if args.workload == "bounce":
+    if args.workload != "direct":
         vin = vis_scat_in.double() / K
         vout = vis_scat_out.double() / K
         visible_paths = vis_direct_total + float((vin * vout).sum().item())
     else:
         visible_paths = vis_direct_total
-    rays = N * M + (N * Pn + Pn * M if args.workload == "bounce" else 0)
+    rays = N * M + (N * Pn + Pn * M if args.workload != "direct" else 0)
     res = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 (visibility bit-specified FP32; field FP32 with FP64 phase)", "data": "synthetic",
@@ -215,7 +223,7 @@ def run_ours(args, rank, world):
            "visible_paths_per_step": visible_paths, "visible_paths_per_s": visible_paths * world * K / (total_ms / 1e3),
            "rays_per_s": rays * world * K / (total_ms / 1e3), "gpu_launches": launches}
     # roofline of the dominant kernel (scatter->sink grid stage; direct stage for the direct workload)
-    if args.workload == "bounce":
+    if args.workload != "direct":
         s2_ms = sum(a.elapsed_time(b) for a, b in ev["s2_list"]) / K
         tests = int(cnt_s2[1].item()) / K
         kernel = "grid_stage_kernel (scatter->sink stage incl. its partial-sum reduction)"
@@ -251,7 +259,7 @@ def run_e2e(args, s, paths):
     ap = Mesh(s.src, point_data={"Normals": s.src_n, "Area": np.ones(s.src.shape[0], np.float32)})
     sk = Mesh(s.snk, point_data={"Normals": s.snk_n})
     sc = Mesh(s.scat, point_data={"Normals": s.scat_n}) if s.scat.shape[0] else None
-    scattering = 1 if args.workload == "bounce" else 0
+    scattering = 0 if args.workload == "direct" else 1
     axis = np.array([1.0, 0.0, 0.0])
 
     def call():

@@ -109,6 +109,14 @@ LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *or
                             const int32_t *dims3, const int32_t *d_tri_offsets, int64_t n_refs,
                             int32_t *d_cell_start, float *d_cell_tris, void *d_ws, size_t ws_bytes, void *stream);
 
+/* Spatial (Morton / Z-order) order of a point set: d_order[n_points] lists the
+ * point indices so that consecutive entries are close in space.  Passed to
+ * lyem_pair_stage as d_src_order / d_snk_order it makes the rays of a warp
+ * coherent.  No counterpart in the reference (it processes pairs in index order). */
+LYEM_API size_t lyem_spatial_order_workspace(int64_t n_points);
+LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t *d_order, void *d_ws,
+                                size_t ws_bytes, void *stream);
+
 /* ------------------------------------------------------------- pair stage */
 
 /* Visibility + fused field for every (source n, sink m) pair:
@@ -130,7 +138,15 @@ LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *or
  * d_counters uint64[2] incremented by (visible pairs, ray/triangle tests),
  * d_src_visible int32[n_src] / d_snk_visible int32[n_snk] incremented by the
  * visible pairs of each source / sink.
- * src_chunk: sources per thread block (0 = automatic). */
+ * d_src_order / d_snk_order (NULL = index order): permutations from
+ * lyem_spatial_order that set which sources share a thread block and which
+ * sinks share a warp; results are unchanged (sink sums are summed in chunk
+ * order, so a different source order can change the last bits of the field).
+ * src_chunk: sources per thread block (0 = automatic; at most 32 for brute
+ * force, 64 for the grid).  traversal (grid only): 0 = automatic, 1 = all lanes
+ * of a warp trace the same source in lockstep, k in 2..33 = each lane moves on
+ * to its next source when its ray ends, new rays being started in batches once
+ * k-1 lanes of the warp are idle. */
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
                                           int32_t src_chunk);
 LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const float *d_src_W, int64_t n_src,
@@ -139,7 +155,8 @@ LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const
                              const float *grid_origin3, float grid_cell, const int32_t *grid_dims3, double alpha,
                              double beta, int32_t self_to_self, int32_t cull, float eps, float *d_sink_out,
                              int32_t accumulate, float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
-                             int32_t *d_src_visible, int32_t *d_snk_visible, int32_t src_chunk, void *d_ws,
+                             int32_t *d_src_visible, int32_t *d_snk_visible, const int32_t *d_src_order,
+                             const int32_t *d_snk_order, int32_t src_chunk, int32_t traversal, void *d_ws,
                              size_t ws_bytes, void *stream);
 
 /* Expands a bit mask [n_src, ceil(n_snk/32)] to bytes [n_src, n_snk] (0/1). */

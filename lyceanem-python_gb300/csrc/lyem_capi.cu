@@ -90,16 +90,22 @@ bool valid_grid(const float* origin3, float cell, const int32_t* dims3) {
     return nc < (1LL << 30);
 }
 
+// Sources per thread block when the caller passes 0.  Brute force: as many
+// as keep about four waves of blocks in flight (the triangle tiles are
+// re-staged per block).  Grid: 16, measured flat between 8 and 32 on the
+// 28 GHz one-bounce scene, fewer when that would leave under four waves.
 int auto_src_chunk(long long n_src, long long n_snk, bool grid) {
     const long long tiles = (n_snk + stage_block_threads() - 1) / stage_block_threads();
-    const long long target = grid ? 152LL * 16 * 4 : 152LL * 8 * 4;
-    long long c = (n_src * tiles) / target;
-    const long long cap = grid ? 256 : brute_max_src_chunk();
-    c = std::max(1LL, std::min(c, cap));
-    // gridDim.y limit
-    const long long min_c = (n_src + 65534) / 65535;
-    if (c < min_c) c = min_c;
-    return (int)c;
+    const long long waves = 152LL * 8 * 4;
+    long long c;
+    if (grid) {
+        c = 16;
+        while (c > 1 && ((n_src + c - 1) / c) * tiles < waves) c /= 2;
+    } else {
+        c = (n_src * tiles) / waves;
+    }
+    const long long cap = grid ? grid_max_src_chunk() : brute_max_src_chunk();
+    return (int)std::max(1LL, std::min(c, cap));
 }
 
 size_t stage_ws_bytes(long long n_src, long long n_snk, int chunk) {
@@ -256,12 +262,27 @@ LYEM_API int lyem_grid_fill(const float* d_tris, int64_t n_tris, const float* or
     return LYEM_OK;
 }
 
+LYEM_API size_t lyem_spatial_order_workspace(int64_t n_points) {
+    return spatial_order_workspace_bytes(n_points < 0 ? 0 : n_points);
+}
+
+LYEM_API int lyem_spatial_order(const float* d_points, int64_t n_points, int32_t* d_order, void* d_ws,
+                                size_t ws_bytes, void* stream) {
+    if (n_points < 0) return LYEM_ERR_INVALID;
+    if (n_points == 0) return LYEM_OK;
+    if (!d_points || !d_order) return LYEM_ERR_INVALID;
+    if (n_points >= (1LL << 31) - 64) return LYEM_ERR_OVERFLOW;
+    if (!d_ws || ws_bytes < spatial_order_workspace_bytes(n_points)) return LYEM_ERR_WORKSPACE;
+    LYEM_CK(spatial_order(d_points, n_points, d_order, d_ws, as_stream(stream)));
+    return LYEM_OK;
+}
+
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
                                           int32_t src_chunk) {
     (void)n_tris;
     if (n_src <= 0 || n_snk <= 0) return 256;
     int chunk = src_chunk > 0 ? src_chunk : auto_src_chunk(n_src, n_snk, use_grid != 0);
-    if (!use_grid) chunk = std::min(chunk, brute_max_src_chunk());
+    chunk = std::min(chunk, use_grid ? grid_max_src_chunk() : brute_max_src_chunk());
     return stage_ws_bytes(n_src, n_snk, chunk);
 }
 
@@ -271,7 +292,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
                              const float* grid_origin3, float grid_cell, const int32_t* grid_dims3, double alpha,
                              double beta, int32_t self_to_self, int32_t cull, float eps, float* d_sink_out,
                              int32_t accumulate, float* d_pair_out, uint32_t* d_mask_bits, uint64_t* d_counters,
-                             int32_t* d_src_visible, int32_t* d_snk_visible, int32_t src_chunk, void* d_ws,
+                             int32_t* d_src_visible, int32_t* d_snk_visible, const int32_t* d_src_order,
+                             const int32_t* d_snk_order, int32_t src_chunk, int32_t traversal, void* d_ws,
                              size_t ws_bytes, void* stream) {
     if (n_src < 0 || n_snk < 0 || n_tris < 0) return LYEM_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
@@ -292,8 +314,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
         ((uintptr_t)d_sink_out & 7u))
         return LYEM_ERR_INVALID;
     int chunk = src_chunk > 0 ? src_chunk : auto_src_chunk(n_src, n_snk, use_grid);
-    if (!use_grid) chunk = std::min(chunk, brute_max_src_chunk());
-    if ((n_src + chunk - 1) / chunk > 65535) return LYEM_ERR_INVALID;
+    chunk = std::min(chunk, use_grid ? grid_max_src_chunk() : brute_max_src_chunk());
+    if ((n_snk + stage_block_threads() - 1) / stage_block_threads() > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
     const size_t need = stage_ws_bytes(n_src, n_snk, chunk);
     if (!d_ws || ws_bytes < need) return LYEM_ERR_WORKSPACE;
 
@@ -332,6 +354,12 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     p.counters = reinterpret_cast<unsigned long long*>(d_counters);
     p.src_visible = d_src_visible;
     p.snk_visible = d_snk_visible;
+    p.src_order = d_src_order;
+    p.snk_order = d_snk_order;
+    if (traversal < 0 || traversal > 33) return LYEM_ERR_INVALID;
+    p.refill_lanes = traversal >= 2 ? traversal - 1 : 0;
+    if (d_mask_bits && d_snk_order)  // permuted sinks set their mask bits one by one
+        LYEM_CK(cudaMemsetAsync(d_mask_bits, 0, sizeof(uint32_t) * (size_t)n_src * (size_t)p.mask_words, s));
     LYEM_CK(launch_pair_stage(p, cull, s));
     if (d_sink_out) {
         const long long chunks = (n_src + chunk - 1) / chunk;
@@ -505,7 +533,7 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
                              n_end, dt.as<float>(), n_tris, grid_on ? dstart.as<int32_t>() : nullptr,
                              grid_on ? dcell.as<float>() : nullptr, org, cell, dims, (double)alpha, (double)beta,
                              not_self_to_self, 1, kEpsilon, nullptr, 0, dpair.as<float>(), nullptr, nullptr, nullptr,
-                             nullptr, 0, dws.p, ws, s);
+                             nullptr, nullptr, nullptr, 0, 0, dws.p, ws, s);
     if (st != LYEM_OK) return st;
     LYEM_CK(cudaMemcpyAsync(out, dpair.p, pair_bytes, cudaMemcpyDeviceToHost, s));
     LYEM_CK(cudaStreamSynchronize(s));

@@ -336,6 +336,98 @@ __global__ void gather_index_kernel(const int* __restrict__ tri_index, const int
     }
 }
 
+// ------------------------------------------------------- spatial order
+// Morton (Z-order) sort of a point set: consecutive entries of the order are
+// close in space, so a warp or block given consecutive points traces coherent rays.
+__global__ void points_bounds_kernel(const float* __restrict__ pts, long long n, float* bounds6) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float v = pts[3 * i + k];
+            lo[k] = fminf(lo[k], v);
+            hi[k] = fmaxf(hi[k], v);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_down_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_down_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 6; ++k) {
+            float v = k < 3 ? lo[k] : hi[k - 3];
+            int bits = __float_as_int(v);
+            int key = bits >= 0 ? bits : (bits ^ 0x7fffffff);
+            if (k < 3) atomicMin(reinterpret_cast<int*>(bounds6) + k, key);
+            else atomicMax(reinterpret_cast<int*>(bounds6) + k, key);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned spread10(unsigned x) {
+    x &= 1023u;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void morton_kernel(const float* __restrict__ pts, long long n, const float* __restrict__ bounds6,
+                              int* keys, int* vals) {
+    float lo[3], sc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = bounds6[k];
+        float ext = bounds6[3 + k] - lo[k];
+        sc[k] = ext > 0.f ? 1023.f / ext : 0.f;
+    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        unsigned c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float q = (pts[3 * i + k] - lo[k]) * sc[k];
+            q = fminf(fmaxf(q, 0.f), 1023.f);
+            if (!(q == q)) q = 0.f;
+            c[k] = (unsigned)q;
+        }
+        keys[i] = (int)(spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2));
+        vals[i] = (int)i;
+    }
+}
+
+size_t spatial_order_workspace_bytes(long long n) {
+    const long long nblocks = (n + kSortTile - 1) / kSortTile;
+    size_t ints = 64 + (size_t)4 * (n + 64) + (size_t)2 * (256 * nblocks + 64) + scan_workspace_ints(256 * nblocks);
+    return ints * sizeof(int) + 256;
+}
+
+cudaError_t spatial_order(const float* pts, long long n, int* order, void* ws, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    float* bounds = static_cast<float*>(ws);
+    int* k0 = static_cast<int*>(ws) + 64;
+    int* v0 = k0 + n + 64;
+    int* k1 = v0 + n + 64;
+    int* v1 = k1 + n + 64;
+    const long long nblocks = (n + kSortTile - 1) / kSortTile;
+    int* hist = v1 + n + 64;
+    int* hist_scanned = hist + 256 * nblocks + 64;
+    int* scan_ws = hist_scanned + 256 * nblocks + 64;
+    bounds_init_kernel<<<1, 32, 0, stream>>>(bounds); note_launches(1);
+    long long b = (n + 255) / 256;
+    b = b > 152 * 8 ? 152 * 8 : b;
+    points_bounds_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, bounds); note_launches(1);
+    bounds_decode_kernel<<<1, 32, 0, stream>>>(bounds); note_launches(1);
+    morton_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, bounds, k0, v0); note_launches(1);
+    bool first = true;
+    cudaError_t e = radix_sort_pairs(k0, v0, k1, v1, n, 1 << 30, hist, hist_scanned, scan_ws, &first, stream);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(order, first ? v0 : v1, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, stream);
+}
+
 static unsigned grid_blocks(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
     if (b < 1) b = 1;

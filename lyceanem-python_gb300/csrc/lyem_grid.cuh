@@ -21,6 +21,9 @@ struct BinSpec {
 size_t scan_workspace_ints(long long n);
 cudaError_t exclusive_scan(const int* in, int* out, long long n, int* ws, cudaStream_t stream);
 
+size_t spatial_order_workspace_bytes(long long n);
+cudaError_t spatial_order(const float* pts, long long n, int* order, void* ws, cudaStream_t stream);
+
 size_t grid_count_workspace_bytes(long long n_tris);
 cudaError_t grid_count(const BinSpec& b, const float4* tris, long long n_tris, int* tri_offsets,
                        unsigned long long* total, void* ws, cudaStream_t stream);

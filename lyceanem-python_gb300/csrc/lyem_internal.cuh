@@ -44,8 +44,15 @@ struct StageParams {
     double beta_d;
     float eps;
     int skip_diag;
-    // launch shape
+    // processing order (nullptr = natural): the thread block handles the
+    // sources src_order[chunk] and the sinks snk_order[tile], so spatially
+    // sorted orders give coherent warps; results are indexed by the original ids
+    const int* src_order;
+    const int* snk_order;
+    // launch shape: blockIdx.y + chunk_base is the source chunk
     int src_chunk;
+    long long chunk_base;
+    int refill_lanes;  // grid stage schedule: 0 = lockstep, k > 0 = batched refill once k lanes are idle
     // outputs
     float* partial;              // [n_chunks, n_snk, 6]
     float* pair_out;             // [n_src, n_snk, 6] or nullptr
@@ -69,6 +76,7 @@ cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, lon
                                    int accumulate, cudaStream_t stream);
 int stage_block_threads();
 int brute_max_src_chunk();
+int grid_max_src_chunk();
 
 // Grid build (lyem_grid.cu).
 cudaError_t launch_tris_bounds(const float4* tris, long long n_tris, float* bounds6, cudaStream_t stream);

@@ -43,6 +43,7 @@ __global__ void fma_probe_kernel(long long iters, float seed, float* sink) {
     float a0 = seed + threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
     float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
     const float b = 0.999999f, c = 1e-7f;
+#pragma unroll 16
     for (long long i = 0; i < iters; ++i) {
         a0 = __fmaf_rn(a0, b, c); a1 = __fmaf_rn(a1, b, c); a2 = __fmaf_rn(a2, b, c); a3 = __fmaf_rn(a3, b, c);
         a4 = __fmaf_rn(a4, b, c); a5 = __fmaf_rn(a5, b, c); a6 = __fmaf_rn(a6, b, c); a7 = __fmaf_rn(a7, b, c);
@@ -97,10 +98,12 @@ cudaError_t read_clear_device_errors(unsigned int* flags, cudaStream_t stream) {
 
 constexpr int kThreads = 128;
 constexpr int kTile = 128;
-constexpr int kBruteMaxChunk = 32;
+constexpr int kBruteMaxChunk = 32;  // one bit per source in a 32-bit mask
+constexpr int kGridMaxChunk = 64;   // one bit per source in a 64-bit mask
 
 int stage_block_threads() { return kThreads; }
 int brute_max_src_chunk() { return kBruteMaxChunk; }
+int grid_max_src_chunk() { return kGridMaxChunk; }
 
 struct BruteSmem {
     float4 raw[2][kTile * 3];
@@ -154,9 +157,13 @@ template <bool MASK_OUT>
 __device__ __forceinline__ void record_visibility(const StageParams& p, long long n, long long m, bool vis) {
     if (!MASK_OUT && !p.src_visible) return;
     unsigned b = __ballot_sync(0xffffffffu, vis);
+    if (MASK_OUT && p.snk_order) {
+        // permuted sinks: the warp's lanes are not 32 consecutive sinks (mask zeroed by the host)
+        if (vis) atomicOr(p.mask_bits + n * p.mask_words + (m >> 5), 1u << (m & 31));
+    }
     if ((threadIdx.x & 31) == 0) {
         long long w = m >> 5;
-        if (MASK_OUT && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
+        if (MASK_OUT && !p.snk_order && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
         if (p.src_visible && b) atomicAdd(p.src_visible + n, __popc(b));
     }
 }
@@ -164,7 +171,7 @@ __device__ __forceinline__ void record_visibility(const StageParams& p, long lon
 __device__ __forceinline__ void flush_block(const StageParams& p, long long m, bool m_ok, const float* acc,
                                             unsigned long long vis_count, unsigned long long tests) {
     if (m_ok) {
-        float2* dst = reinterpret_cast<float2*>(p.partial + 6 * ((long long)blockIdx.y * p.n_snk + m));
+        float2* dst = reinterpret_cast<float2*>(p.partial + 6 * ((p.chunk_base + (long long)blockIdx.y) * p.n_snk + m));
         dst[0] = make_float2(acc[0], acc[1]);
         dst[1] = make_float2(acc[2], acc[3]);
         dst[2] = make_float2(acc[4], acc[5]);
@@ -189,11 +196,15 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     BruteSmem& sm = *reinterpret_cast<BruteSmem*>(smem_raw);
 
     const int tid = threadIdx.x;
-    const long long m = (long long)blockIdx.x * kThreads + tid;
-    const bool m_ok = m < p.n_snk;
-    const long long n0 = (long long)blockIdx.y * p.src_chunk;
+    const long long ms = (long long)blockIdx.x * kThreads + tid;
+    const bool m_ok = ms < p.n_snk;
+    const long long m = m_ok ? (p.snk_order ? (long long)p.snk_order[ms] : ms) : 0;
+    const long long n0 = (p.chunk_base + (long long)blockIdx.y) * p.src_chunk;
     const long long rem = p.n_src - n0;
     const int nsrc = (int)(rem < p.src_chunk ? rem : p.src_chunk);
+    auto src_index = [&](int s) -> long long {
+        return p.src_order ? (long long)p.src_order[n0 + s] : n0 + s;
+    };
 
     float ex = 0.f, ey = 0.f, ez = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
     if (m_ok) {
@@ -202,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     }
     uint32_t pending = 0, blocked = 0;
     for (int s = 0; s < nsrc; ++s)
-        if (m_ok && !(p.skip_diag && n0 + s == m)) pending |= 1u << s;
+        if (m_ok && !(p.skip_diag && src_index(s) == m)) pending |= 1u << s;
 
     const long long T = p.n_tris;
     const int ntiles = (int)((T + kTile - 1) / kTile);
@@ -234,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
         const float4* rt = sm.raw[k & 1];
         for (int s = 0; s < nsrc; ++s) {
             TriPre* pb = sm.pre[(k * nsrc + s) & 1];
-            const float* so = p.src_pos + 3 * (n0 + s);
+            const float* so = p.src_pos + 3 * src_index(s);
             const float ox = so[0], oy = so[1], oz = so[2];
             if (tid < cnt) pb[tid] = make_tripre(ox, oy, oz, rt[3 * tid], rt[3 * tid + 1], rt[3 * tid + 2]);
             const bool mine = (pending >> s) & 1u;
@@ -276,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     unsigned long long vis_count = 0;
     for (int s = 0; s < nsrc; ++s) {
-        const long long n = n0 + s;
+        const long long n = src_index(s);
         const bool vis = m_ok && !((blocked >> s) & 1u);
         record_visibility<MASK_OUT>(p, n, m, vis);
         const float* so = p.src_pos + 3 * n;
@@ -286,99 +297,182 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     flush_block(p, m, m_ok, acc, vis_count, tests);
 }
 
-// Any-hit walk of the segment o -> o + len*d through the uniform grid.
-template <bool CULL>
-__device__ __forceinline__ bool grid_blocked(const StageParams& p, float ox, float oy, float oz, const Ray& r,
-                                             unsigned long long& tests) {
-    const float o[3] = {ox, oy, oz};
-    const float d[3] = {r.dx, r.dy, r.dz};
-    float inv[3];
-    float t0 = 0.f, t1 = r.len;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (d[k] == 0.f) {
-            inv[k] = 0.f;
-            if (o[k] < p.g0[k] || o[k] > p.g1[k]) return false;
-        } else {
-            inv[k] = 1.0f / d[k];
-            float ta = (p.g0[k] - o[k]) * inv[k], tb = (p.g1[k] - o[k]) * inv[k];
-            t0 = fmaxf(t0, fminf(ta, tb));
-            t1 = fminf(t1, fmaxf(ta, tb));
-        }
+// Grid stage.  Each lane owns one sink and resolves the rays from the chunk's
+// sources to it.  A ray walks the uniform grid (Amanatides-Woo; the boundary
+// crossings are recomputed from the cell index, so no error accumulates) and
+// tests the triangles stored contiguously per cell (float4 loads), stopping at
+// its first hit.  Two schedules of the rays over the lanes:
+//   lockstep  all lanes of a warp trace source s, then source s + 1, ...; ray
+//             set-up runs in lockstep, a warp waits for its longest ray;
+//   refill    each lane moves to its next source when its ray ends, but new
+//             rays are started in batches (once `refill_lanes` lanes of the
+//             warp are idle, or none is busy) so the set-up code is not
+//             serialised lane by lane.
+// Visibility of the chunk is kept as a 64-bit blocked mask; the field epilogue
+// then runs over the sources in lockstep.
+struct Walk {
+    float ox, oy, oz;
+    Ray r;
+    float ix, iy, iz, t1;
+    int cx, cy, cz, q, q1, guard;
+};
+
+// Starts the walk of segment o -> e; false if the segment misses the grid box.
+__device__ __forceinline__ bool walk_begin(const StageParams& p, Walk& w, float ox, float oy, float oz, float ex,
+                                           float ey, float ez) {
+    w.ox = ox; w.oy = oy; w.oz = oz;
+    w.r = make_ray(ox, oy, oz, ex, ey, ez);
+    float t0 = 0.f;
+    w.t1 = w.r.len;
+    bool miss = false;
+#define LYEM_SLAB(D, O, G0, G1, INV)                       \
+    if (D == 0.f) {                                        \
+        INV = 0.f;                                         \
+        if (O < G0 || O > G1) miss = true;                 \
+    } else {                                               \
+        INV = 1.0f / D;                                    \
+        float ta = (G0 - O) * INV, tb = (G1 - O) * INV;    \
+        t0 = fmaxf(t0, fminf(ta, tb));                     \
+        w.t1 = fminf(w.t1, fmaxf(ta, tb));                 \
     }
-    if (!(t0 <= t1)) return false;
-    int idx[3], step[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        float q = (o[k] + t0 * d[k] - p.g0[k]) * p.inv_cell;
-        int i = (int)floorf(q);
-        i = i < 0 ? 0 : (i > p.dims[k] - 1 ? p.dims[k] - 1 : i);
-        idx[k] = i;
-        step[k] = d[k] > 0.f ? 1 : (d[k] < 0.f ? -1 : 0);
-    }
-    const int nx = p.dims[0], nxy = p.dims[0] * p.dims[1];
-    // A monotone walk visits at most dims[0] + dims[1] + dims[2] cells.
-    int guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
-    while (true) {
-        if (--guard < 0) {
-            atomicOr(&g_device_error, 2u);
-            return false;
-        }
-        const int c = idx[2] * nxy + idx[1] * nx + idx[0];
-        const int r0 = __ldg(p.cell_start + c), r1 = __ldg(p.cell_start + c + 1);
-        for (int q = r0; q < r1; ++q) {
-            const float4* t = p.cell_tris + 3 * (long long)q;
-            const float4 v0 = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
-            if (hit_full<CULL>(r, ox, oy, oz, v0, e1, e2, p.eps)) {
-                tests += (unsigned long long)(q - r0 + 1);
-                return true;
-            }
-        }
-        tests += (unsigned long long)(r1 - r0);
-        // parameter of the next boundary crossing on each axis, from the index
-        float tn[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            if (step[k] == 0) {
-                tn[k] = __int_as_float(0x7f800000);
-            } else {
-                float b = p.g0[k] + (float)(idx[k] + (step[k] > 0)) * p.cell;
-                tn[k] = (b - o[k]) * inv[k];
-            }
-        }
-        int a = (tn[0] < tn[1]) ? (tn[0] < tn[2] ? 0 : 2) : (tn[1] < tn[2] ? 1 : 2);
-        if (tn[a] > t1) return false;
-        idx[a] += step[a];
-        if (idx[a] < 0 || idx[a] >= p.dims[a]) return false;
-    }
+    LYEM_SLAB(w.r.dx, ox, p.g0[0], p.g1[0], w.ix)
+    LYEM_SLAB(w.r.dy, oy, p.g0[1], p.g1[1], w.iy)
+    LYEM_SLAB(w.r.dz, oz, p.g0[2], p.g1[2], w.iz)
+#undef LYEM_SLAB
+    if (miss || !(t0 <= w.t1)) return false;
+    w.cx = min(max((int)floorf((ox + t0 * w.r.dx - p.g0[0]) * p.inv_cell), 0), p.dims[0] - 1);
+    w.cy = min(max((int)floorf((oy + t0 * w.r.dy - p.g0[1]) * p.inv_cell), 0), p.dims[1] - 1);
+    w.cz = min(max((int)floorf((oz + t0 * w.r.dz - p.g0[2]) * p.inv_cell), 0), p.dims[2] - 1);
+    w.guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
+    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
+    w.q = __ldg(p.cell_start + c);
+    w.q1 = __ldg(p.cell_start + c + 1);
+    return true;
 }
 
-template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT>
+// Tests triangle q of the current cell and advances q; true on a hit.
+template <bool CULL>
+__device__ __forceinline__ bool walk_test(const StageParams& p, Walk& w) {
+    const float4* t = p.cell_tris + 3 * (long long)w.q;
+    const float4 v0 = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
+    ++w.q;
+    return hit_full<CULL>(w.r, w.ox, w.oy, w.oz, v0, e1, e2, p.eps);
+}
+
+// Crosses the nearest cell boundary; false when the segment or the grid ends there.
+__device__ __forceinline__ bool walk_step(const StageParams& p, Walk& w) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float cell = p.cell;
+    const float tx = w.r.dx > 0.f ? (p.g0[0] + (float)(w.cx + 1) * cell - w.ox) * w.ix
+                                  : (w.r.dx < 0.f ? (p.g0[0] + (float)w.cx * cell - w.ox) * w.ix : kInf);
+    const float ty = w.r.dy > 0.f ? (p.g0[1] + (float)(w.cy + 1) * cell - w.oy) * w.iy
+                                  : (w.r.dy < 0.f ? (p.g0[1] + (float)w.cy * cell - w.oy) * w.iy : kInf);
+    const float tz = w.r.dz > 0.f ? (p.g0[2] + (float)(w.cz + 1) * cell - w.oz) * w.iz
+                                  : (w.r.dz < 0.f ? (p.g0[2] + (float)w.cz * cell - w.oz) * w.iz : kInf);
+    bool done;
+    if (tx <= ty && tx <= tz) {
+        w.cx += w.r.dx > 0.f ? 1 : -1;
+        done = tx > w.t1 || w.cx < 0 || w.cx >= p.dims[0];
+    } else if (ty <= tz) {
+        w.cy += w.r.dy > 0.f ? 1 : -1;
+        done = ty > w.t1 || w.cy < 0 || w.cy >= p.dims[1];
+    } else {
+        w.cz += w.r.dz > 0.f ? 1 : -1;
+        done = tz > w.t1 || w.cz < 0 || w.cz >= p.dims[2];
+    }
+    if (--w.guard < 0) {  // a monotone walk visits at most dims[0] + dims[1] + dims[2] cells
+        atomicOr(&g_device_error, 2u);
+        done = true;
+    }
+    if (done) return false;
+    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
+    w.q = __ldg(p.cell_start + c);
+    w.q1 = __ldg(p.cell_start + c + 1);
+    return true;
+}
+
+constexpr int kLockstep = 0;
+constexpr int kRefill = 1;
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, int MODE>
 __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams p) {
     const int tid = threadIdx.x;
-    const long long m = (long long)blockIdx.x * kThreads + tid;
-    const bool m_ok = m < p.n_snk;
-    const long long n0 = (long long)blockIdx.y * p.src_chunk;
+    const long long ms = (long long)blockIdx.x * kThreads + tid;
+    const bool m_ok = ms < p.n_snk;
+    const long long m = m_ok ? (p.snk_order ? (long long)p.snk_order[ms] : ms) : 0;
+    const long long n0 = (p.chunk_base + (long long)blockIdx.y) * p.src_chunk;
     const long long rem = p.n_src - n0;
     const int nsrc = (int)(rem < p.src_chunk ? rem : p.src_chunk);
-    float ex = 0.f, ey = 0.f, ez = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    auto src_index = [&](int s) -> long long {
+        return p.src_order ? (long long)p.src_order[n0 + s] : n0 + s;
+    };
+    float ex = 0.f, ey = 0.f, ez = 0.f;
     if (m_ok) {
         ex = p.snk_pos[3 * m]; ey = p.snk_pos[3 * m + 1]; ez = p.snk_pos[3 * m + 2];
+    }
+    unsigned long long blocked = 0, tests = 0;
+    Walk w;
+    if (MODE == kLockstep) {
+        for (int s = 0; s < nsrc; ++s) {
+            const long long n = src_index(s);
+            if (!m_ok || (p.skip_diag && n == m)) continue;
+            const float* so = p.src_pos + 3 * n;
+            if (!walk_begin(p, w, so[0], so[1], so[2], ex, ey, ez)) continue;
+            bool hit = false;
+            while (true) {
+                while (w.q < w.q1) {
+                    ++tests;
+                    if (walk_test<CULL>(p, w)) { hit = true; break; }
+                }
+                if (hit || !walk_step(p, w)) break;
+            }
+            if (hit) blocked |= 1ull << s;
+        }
+    } else {
+        int s = -1;
+        bool has = false;
+        // next source of this lane that needs a walk (untested and off-grid rays are visible)
+        auto refill = [&]() {
+            while (++s < nsrc) {
+                const long long n = src_index(s);
+                if (p.skip_diag && n == m) continue;
+                const float* so = p.src_pos + 3 * n;
+                if (walk_begin(p, w, so[0], so[1], so[2], ex, ey, ez)) { has = true; return; }
+            }
+        };
+        const unsigned full = 0xffffffffu;
+        while (true) {
+            const bool can = !has && m_ok && s + 1 < nsrc;
+            const unsigned busy = __ballot_sync(full, has);
+            const unsigned idle = __ballot_sync(full, can);
+            if (busy == 0 && idle == 0) break;
+            if (can && (busy == 0 || __popc(idle) >= p.refill_lanes)) refill();
+            if (has) {
+                while (w.q < w.q1) {
+                    ++tests;
+                    if (walk_test<CULL>(p, w)) {
+                        blocked |= 1ull << s;
+                        has = false;
+                        break;
+                    }
+                }
+                if (has && !walk_step(p, w)) has = false;
+            }
+        }
+    }
+
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    if (m_ok) {
         nx = p.snk_nrm[3 * m]; ny = p.snk_nrm[3 * m + 1]; nz = p.snk_nrm[3 * m + 2];
     }
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    unsigned long long vis_count = 0, tests = 0;
-    for (int s = 0; s < nsrc; ++s) {
-        const long long n = n0 + s;
-        const float* so = p.src_pos + 3 * n;
-        const float ox = so[0], oy = so[1], oz = so[2];
-        bool vis = m_ok;
-        if (m_ok && !(p.skip_diag && n == m)) {
-            const Ray r = make_ray(ox, oy, oz, ex, ey, ez);
-            vis = !grid_blocked<CULL>(p, ox, oy, oz, r, tests);
-        }
+    unsigned long long vis_count = 0;
+    for (int k = 0; k < nsrc; ++k) {
+        const long long n = src_index(k);
+        const bool vis = m_ok && !((blocked >> k) & 1ull);
         record_visibility<MASK_OUT>(p, n, m, vis);
-        pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, ox, oy, oz, ex, ey, ez, nx, ny, nz, acc);
+        const float* so = p.src_pos + 3 * n;
+        pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;
     }
     flush_block(p, m, m_ok, acc, vis_count, tests);
@@ -395,19 +489,31 @@ __global__ void reduce_partials_kernel(const float* __restrict__ partial, long l
 }
 
 template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT>
-static cudaError_t launch_t(const StageParams& p, cudaStream_t stream) {
-    const long long chunks = (p.n_src + p.src_chunk - 1) / p.src_chunk;
-    dim3 grid((unsigned)((p.n_snk + kThreads - 1) / kThreads), (unsigned)chunks);
-    if (p.cell_start) {
-        grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT><<<grid, kThreads, 0, stream>>>(p); note_launches(1);
-    } else {
-        const size_t smem = sizeof(BruteSmem);
-        auto kern = brute_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
+    const long long chunks = (p0.n_src + p0.src_chunk - 1) / p0.src_chunk;
+    const unsigned tiles = (unsigned)((p0.n_snk + kThreads - 1) / kThreads);
+    // gridDim.y is limited to 65535: launch the source chunks in slices
+    for (long long base = 0; base < chunks; base += 65535) {
+        StageParams p = p0;
+        p.chunk_base = base;
+        dim3 grid(tiles, (unsigned)(chunks - base < 65535 ? chunks - base : 65535));
+        if (p.cell_start) {
+            if (p.refill_lanes > 0)
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kRefill><<<grid, kThreads, 0, stream>>>(p);
+            else
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep><<<grid, kThreads, 0, stream>>>(p);
+            note_launches(1);
+        } else {
+            const size_t smem = sizeof(BruteSmem);
+            auto kern = brute_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT>;
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            kern<<<grid, kThreads, smem, stream>>>(p); note_launches(1);
+        }
+        cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        kern<<<grid, kThreads, smem, stream>>>(p); note_launches(1);
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 template <bool CULL, bool WEIGHTED, bool PAIR_OUT>

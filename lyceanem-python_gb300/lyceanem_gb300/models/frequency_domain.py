@@ -48,10 +48,15 @@ def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=Non
     dev = structure.device
     kw = dict(tris=dev.tris, grid=dev.grid, alpha=alpha, beta=beta, self_to_self=False, counters=counters, cull=cull,
               eps=eps)
+    # Processing order: scatter points (unstructured) are traced in Morton
+    # order; sources and sinks keep the caller's order, which for arrays and
+    # elevation-major far-field grids already puts rays of similar cost in a warp.
     out = P.pair_stage(src, E, snk, snk_n, **kw).sink
     if scattering >= 1 and scat is not None and len(scat):
-        e_p = P.pair_stage(src, E, scat, scat_n, **kw).sink
-        P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, **kw)
+        scat = P._points(scat)
+        o_scat = P.spatial_order(scat)
+        e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, **kw).sink
+        P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat, **kw)
     return out
 
 

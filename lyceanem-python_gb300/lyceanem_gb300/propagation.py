@@ -131,7 +131,8 @@ class StageResult:
 
 def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, grid=None, src_W=None,
                self_to_self=False, cull=True, eps=EPSILON, sink_out=None, accumulate=False, want_pairs=False,
-               want_mask=False, counters=None, src_visible=None, snk_visible=None, src_chunk=0, workspace=None):
+               want_mask=False, counters=None, src_visible=None, snk_visible=None, src_order=None, snk_order=None,
+               src_chunk=0, traversal=0, workspace=None):
     """Visibility + fused field of every (source, sink) pair.
 
     Returns a StageResult whose .sink is complex64 [n_snk,3] with
@@ -141,6 +142,10 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     counters (int64 [2]) accumulates (visible pairs, ray/triangle tests);
     src_visible / snk_visible (int32 [n_src] / [n_snk]) accumulate visible pairs
     per source / per sink.
+    src_order / snk_order (int32, e.g. from spatial_order) set the processing
+    order only: which sources share a thread block and which sinks a warp.
+    src_chunk / traversal choose the launch shape and the ray schedule of the
+    grid kernel (0 = automatic; see lyem_pair_stage in include/lyem.h).
     Visibility uses `grid` (a UniformGrid) if given, else brute force over
     `tris`.  self_to_self=False reproduces the reference's untested pair
     n == m (lyceanem/src/raycasting_brute_force.cuh:27)."""
@@ -175,10 +180,21 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
                              float(beta), int(bool(self_to_self)), int(bool(cull)), float(eps),
                              _p(torch.view_as_real(sink_out)), int(bool(accumulate)),
                              _p(None if pairs is None else torch.view_as_real(pairs)), _p(mbits), _p(counters),
-                             _p(src_visible), _p(snk_visible), int(src_chunk), _p(workspace), workspace.numel(),
-                             _stream())
+                             _p(src_visible), _p(snk_visible), _p(src_order), _p(snk_order), int(src_chunk),
+                             int(traversal), _p(workspace), workspace.numel(), _stream())
     check(st, "pair_stage")
     return StageResult(sink_out, pairs, mbits, counters, N, M)
+
+
+def spatial_order(points):
+    """Morton order of a point set (int32 permutation, on the device)."""
+    pts = _points(points)
+    n = pts.shape[0]
+    out = torch.empty(n, dtype=torch.int32, device=pts.device)
+    if n:
+        ws = _ws(lib.lyem_spatial_order_workspace(n), pts.device)
+        check(lib.lyem_spatial_order(_p(pts), n, _p(out), _p(ws), ws.numel(), _stream()), "spatial_order")
+    return out
 
 
 def device_errors():

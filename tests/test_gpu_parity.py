@@ -283,3 +283,23 @@ def test_frequency_domain_api():
     et, ep = FD.calculate_farfield(ap, solid, axis, az_range=np.linspace(-180, 180, 9),
                                    el_range=np.linspace(-90, 90, 5), wavelength=0.04, farfield_distance=5.0, beta=beta)
     assert et.shape == (45,) and np.isfinite(et).all() and np.isfinite(ep).all()
+
+
+def test_spatial_order_and_ordered_stages():
+    """A spatial order is a permutation, and ordered stages give the same masks (and fields to rounding)."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(31, n_src=150, n_snk=700, n_tris=600)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    o_src, o_snk = P.spatial_order(src), P.spatial_order(snk)
+    assert sorted(o_snk.cpu().tolist()) == list(range(700))
+    assert sorted(o_src.cpu().tolist()) == list(range(150))
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f))
+    g = P.UniformGrid(tris, cell=0.25)
+    for kw in (dict(tris=tris), dict(grid=g)):
+        a = P.pair_stage(src, E, snk, snk_n, beta=80.0, want_mask=True, want_pairs=True, **kw)
+        b = P.pair_stage(src, E, snk, snk_n, beta=80.0, want_mask=True, want_pairs=True, src_order=o_src,
+                         snk_order=o_snk, **kw)
+        assert np.array_equal(b.mask().cpu().numpy(), om)
+        assert torch.equal(a.pairs, b.pairs)
+        assert rel_err(b.sink.cpu().numpy(), a.sink.cpu().numpy()) < 1e-6
+    _no_device_errors()
