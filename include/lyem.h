@@ -159,6 +159,32 @@ LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const
                              const int32_t *d_snk_order, int32_t src_chunk, int32_t traversal, void *d_ws,
                              size_t ws_bytes, void *stream);
 
+/* lyem_pair_stage for callers that may not allocate device memory (a host
+ * whose own allocator owns all device memory, or code that forbids allocation
+ * calls once running), so cannot pass the stage's scratch buffer.  No
+ * counterpart in the reference (its bindings allocate and free per call).
+ * Same arguments as lyem_pair_stage without d_ws / ws_bytes; the scratch is a
+ * fixed array inside the library of lyem_pair_stage_noalloc_scratch_bytes()
+ * (32 MiB) on every device that loads it.  Limit: the per-chunk partial sums,
+ * ceil(n_src / src_chunk) * n_snk * 24 bytes, must fit in it (src_chunk at most
+ * 32 for brute force, 64 for the grid; with src_chunk = 0 the smallest chunk
+ * that fits is used); larger problems return LYEM_ERR_WORKSPACE and launch
+ * nothing.  The first call on a device looks up the array's device address
+ * and should come before any stream capture.  All calls share the array (it
+ * keeps the last call's contents; nothing in it needs to start at zero), so
+ * calls that overlap on the GPU race.  Calls no allocation routine. */
+LYEM_API size_t lyem_pair_stage_noalloc_scratch_bytes(void);
+LYEM_API int lyem_pair_stage_noalloc(const float *d_src_pos, const float *d_src_E, const float *d_src_W,
+                                     int64_t n_src, const float *d_snk_pos, const float *d_snk_nrm, int64_t n_snk,
+                                     const float *d_tris, int64_t n_tris, const int32_t *d_cell_start,
+                                     const float *d_cell_tris, const float *grid_origin3, float grid_cell,
+                                     const int32_t *grid_dims3, double alpha, double beta, int32_t self_to_self,
+                                     int32_t cull, float eps, float *d_sink_out, int32_t accumulate,
+                                     float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
+                                     int32_t *d_src_visible, int32_t *d_snk_visible, const int32_t *d_src_order,
+                                     const int32_t *d_snk_order, int32_t src_chunk, int32_t traversal,
+                                     void *stream);
+
 /* Expands a bit mask [n_src, ceil(n_snk/32)] to bytes [n_src, n_snk] (0/1). */
 LYEM_API int lyem_mask_to_bytes(const uint32_t *d_mask_bits, int64_t n_src, int64_t n_snk, uint8_t *d_out,
                                 void *stream);

@@ -65,6 +65,10 @@ SIGNATURES = {
                          _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _sz,
                          _vp],
                         ctypes.c_int),
+    "lyem_pair_stage_noalloc_scratch_bytes": ([], _sz),
+    "lyem_pair_stage_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _f32p, _f32, _i32p, _f64,
+                                 _f64, _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32,
+                                 _vp], ctypes.c_int),
     "lyem_mask_to_bytes": ([_vp, _i64, _i64, _vp, _vp], ctypes.c_int),
     "lyem_em_bin_counts": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp], ctypes.c_int),
     "lyem_em_bin_triangles": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp, _i64, _vp], ctypes.c_int),
