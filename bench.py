@@ -34,9 +34,10 @@ sys.path.insert(0, ROOT)
 METRIC = "visible paths/s (mask+field) on 1 GB300; mixed-prec vs FP32 sweep at ≤1e-4 rel err"
 OPS_PER_TEST = 30  # FP32-pipe operations of one Moller-Trumbore test (lyceanem/src/raycasting.cuh:23-59)
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes per launch of the scatter->sink grid-stage kernel, from the ncu capture summarised in
-# profiles/grid_stage_kernel_bounce.md (None until that capture exists).
-GRID_STAGE_DRAM_BYTES = None
+# DRAM bytes (read + write) of one full-size launch of the scatter->sink grid-stage kernel, from the
+# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (117.02 MB + 4.88 GB; the
+# writes are the per-chunk partial sums).
+GRID_STAGE_DRAM_BYTES = 117.02e6 + 4.88e9
 
 
 def parse():
