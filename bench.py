@@ -51,6 +51,7 @@ def parse():
                          "(profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the mixed-precision beam-sweep measurement")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
     return ap.parse_args()
 
@@ -241,6 +242,8 @@ def run_ours(args, rank, world):
                        "share_of_step": s2_ms / ms_per_step}
     if clk:
         res["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_sweep:
+        res["sweep"] = run_sweep(args)
     if rank == 0 and world == 1 and not args.no_e2e:
         res["e2e"] = run_e2e(args, s, paths)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -282,6 +285,69 @@ def run_e2e(args, s, paths):
             "seconds_per_step": dt,
             "api": "lyceanem_gb300.models.frequency_domain.calculate_scattering (host numpy in/out, "
                    "acceleration structure built inside the call)"}
+
+
+# ------------------------------------------------------------------ sweep
+def run_sweep(args, n_check=256, reps=5):
+    """Mixed-precision beam sweep: 64x64 array at 28 GHz, ground + 20,000 clutter triangles, 65,341 sinks,
+    K = 2,048 steering vectors.  Times the three component GEMMs per mode on the formed network and measures
+    each mode's error against an FP64 product on a seeded sample of sinks (oracle network, all beams)."""
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300 import beam_sweep as BS
+    from lyceanem_gb300 import propagation as P
+    from lyceanem_gb300 import scenes
+    from oracle import oracle as O
+    s = scenes.sweep_scene()
+    beta = 2 * np.pi / s.wavelength
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    tris = P.pack_triangles(t(s.verts), t(s.faces))
+    grid = P.UniformGrid(tris, cell=s.cell)
+    N, M, K = s.src.shape[0], s.snk.shape[0], s.weights.shape[0]
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    G = BS.form_network(t(s.src), s.pol, t(s.snk), t(s.snk_n), beta=beta, grid=grid)
+    b.record()
+    torch.cuda.synchronize()
+    form_ms = a.elapsed_time(b)
+    W = t(s.weights)
+    rng = np.random.default_rng(7)
+    pick = np.sort(rng.choice(M, size=n_check, replace=False))
+    flops = 8.0 * M * N * K * 3
+    res = {"n_elements": N, "n_sinks": M, "n_beams": K, "network_form_ms": form_ms,
+           "algorithmic_flops": flops}
+    outs = {}
+    for mode in ("fp32", "bf16x3", "fp16x3"):
+        sw = BS.BeamSweep(G, mode)
+        out = sw.run(W)
+        torch.cuda.synchronize()
+        ev = []
+        for _ in range(reps):
+            x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            x.record()
+            sw.run(W, out=out)
+            y.record()
+            ev.append((x, y))
+        torch.cuda.synchronize()
+        ms = min(x.elapsed_time(y) for x, y in ev)
+        outs[mode] = sw.fields(out)[torch.from_numpy(pick).cuda()].cpu().numpy()
+        res[mode] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12}
+        del sw, out
+        torch.cuda.empty_cache()
+    del G
+    # FP64 reference on the sampled sinks: oracle visibility + FP64 network, FP64 product
+    og = O.Grid(O.pack_triangles(s.verts, s.faces), s.cell)
+    snk, snk_n = s.snk[pick], s.snk_n[pick]
+    mask = og.mask(s.src, snk, self_to_self=True)  # the network tests every pair (sink indices are sampled)
+    G64 = O.pair_field(s.src, np.tile(s.pol, (N, 1)), snk, snk_n, mask, 0.0, beta)
+    E64 = np.einsum("nmc,kn->mkc", G64, s.weights.astype(np.complex128), optimize=True)
+    for mode, E in outs.items():
+        res[mode]["rel_err_fp64"] = float(np.linalg.norm(E - E64) / np.linalg.norm(E64))
+    res["speedup_bf16x3_vs_fp32"] = res["fp32"]["ms"] / res["bf16x3"]["ms"]
+    res["speedup_fp16x3_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3"]["ms"]
+    res["error_sample"] = f"{n_check} seeded sinks x {K} beams x 3 components, relative Frobenius norm"
+    return res
 
 
 # ------------------------------------------------------------------ CPU

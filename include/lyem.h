@@ -189,6 +189,31 @@ LYEM_API int lyem_pair_stage_noalloc(const float *d_src_pos, const float *d_src_
 LYEM_API int lyem_mask_to_bytes(const uint32_t *d_mask_bits, int64_t n_src, int64_t n_snk, uint8_t *d_out,
                                 void *stream);
 
+/* ------------------------------------------------------------ beam sweep */
+
+/* Sink fields of K excitation vectors for a formed network:
+ *   E[m, k, c] = sum_n G[n, m, c] W[k, n]
+ * with G the pair-stage network (d_pair_out of lyem_pair_stage for unit
+ * excitations, complex64 [n_src, n_snk, 3]) and W complex64 [n_beams, n_src].
+ * Replaces re-running the whole model once per excitation
+ * (lyceanem/models/frequency_domain.py:858-921, multiE) and the host GEMMs of
+ * lyceanem/models/frequency_domain.py:258-260.
+ * mode 0: plain complex64 FP32 (cublasCgemm); 1: BF16 split (x = hi + lo,
+ * hi*hi + hi*lo + lo*hi on the tensor cores, FP32 accumulation); 2: FP16 split.
+ * Step 1 converts G into the GEMM operand (d_network, lyem_sweep_network_bytes;
+ * ld >= n_snk, a multiple of 8); step 2 converts W (split modes only, d_B,
+ * lyem_sweep_weights_bytes); step 3 runs the three component GEMMs into d_out,
+ * complex64 [3][n_beams][ldc] (component c, beam k: column-major E[:, k, c];
+ * ldc >= ld, rows n_snk..ld-1 receive zeros). */
+LYEM_API size_t lyem_sweep_network_bytes(int64_t n_src, int64_t ld, int32_t mode);
+LYEM_API size_t lyem_sweep_weights_bytes(int64_t n_src, int64_t n_beams, int32_t mode);
+LYEM_API int lyem_sweep_prepare_network(const float *d_pairs, int64_t n_src, int64_t n_snk, int32_t mode, int64_t ld,
+                                        void *d_network, void *stream);
+LYEM_API int lyem_sweep_prepare_weights(const float *d_W, int64_t n_src, int64_t n_beams, int32_t mode, void *d_B,
+                                        void *stream);
+LYEM_API int lyem_sweep_run(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
+                            const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *stream);
+
 /* ------------------------------------------ host mirrors of lyceanem.em */
 
 /* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):

@@ -153,8 +153,11 @@ __device__ __forceinline__ void pair_epilogue(const StageParams& p, long long n,
 }
 
 // Mask bits of the warp's 32 sinks for source n, and the per-source visible count.
+// ms is the lane's sink slot (m = ms in natural order); lanes past the last
+// sink have vis == false.
 template <bool MASK_OUT>
-__device__ __forceinline__ void record_visibility(const StageParams& p, long long n, long long m, bool vis) {
+__device__ __forceinline__ void record_visibility(const StageParams& p, long long n, long long m, long long ms,
+                                                  bool vis) {
     if (!MASK_OUT && !p.src_visible) return;
     unsigned b = __ballot_sync(0xffffffffu, vis);
     if (MASK_OUT && p.snk_order) {
@@ -162,7 +165,8 @@ __device__ __forceinline__ void record_visibility(const StageParams& p, long lon
         if (vis) atomicOr(p.mask_bits + n * p.mask_words + (m >> 5), 1u << (m & 31));
     }
     if ((threadIdx.x & 31) == 0) {
-        long long w = m >> 5;
+        // natural order: the warp's slots ms .. ms + 31 are the sinks of word ms / 32
+        const long long w = ms >> 5;
         if (MASK_OUT && !p.snk_order && w < p.mask_words) p.mask_bits[n * p.mask_words + w] = b;
         if (p.src_visible && b) atomicAdd(p.src_visible + n, __popc(b));
     }
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
     for (int s = 0; s < nsrc; ++s) {
         const long long n = src_index(s);
         const bool vis = m_ok && !((blocked >> s) & 1u);
-        record_visibility<MASK_OUT>(p, n, m, vis);
+        record_visibility<MASK_OUT>(p, n, m, ms, vis);
         const float* so = p.src_pos + 3 * n;
         pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams 
     for (int k = 0; k < nsrc; ++k) {
         const long long n = src_index(k);
         const bool vis = m_ok && !((blocked >> k) & 1ull);
-        record_visibility<MASK_OUT>(p, n, m, vis);
+        record_visibility<MASK_OUT>(p, n, m, ms, vis);
         const float* so = p.src_pos + 3 * n;
         pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;

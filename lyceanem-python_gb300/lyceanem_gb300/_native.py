@@ -70,6 +70,11 @@ SIGNATURES = {
                                  _f64, _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32,
                                  _vp], ctypes.c_int),
     "lyem_mask_to_bytes": ([_vp, _i64, _i64, _vp, _vp], ctypes.c_int),
+    "lyem_sweep_network_bytes": ([_i64, _i64, _i32], _sz),
+    "lyem_sweep_weights_bytes": ([_i64, _i64, _i32], _sz),
+    "lyem_sweep_prepare_network": ([_vp, _i64, _i64, _i32, _i64, _vp, _vp], ctypes.c_int),
+    "lyem_sweep_prepare_weights": ([_vp, _i64, _i64, _i32, _vp, _vp], ctypes.c_int),
+    "lyem_sweep_run": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_em_bin_counts": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp], ctypes.c_int),
     "lyem_em_bin_triangles": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_em_calculate_scattering_brute_force": (

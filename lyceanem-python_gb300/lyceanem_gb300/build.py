@@ -23,7 +23,9 @@ LIB_PATH = os.path.join(LIB_DIR, "liblyem_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
-LINK_LIBS = ["-lcublas"]
+_CUDA_LIB = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(shutil.which("nvcc") or
+                                                                         "/usr/local/cuda/bin/nvcc"))), "lib64")
+LINK_LIBS = ["-lcublas", "-Xlinker", "-rpath", "-Xlinker", _CUDA_LIB]
 
 
 def _nvcc():

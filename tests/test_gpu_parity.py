@@ -303,3 +303,26 @@ def test_spatial_order_and_ordered_stages():
         assert torch.equal(a.pairs, b.pairs)
         assert rel_err(b.sink.cpu().numpy(), a.sink.cpu().numpy()) < 1e-6
     _no_device_errors()
+
+
+@pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3", 1e-4), ("fp16x3", 1e-5)])
+def test_beam_sweep_modes_against_fp64(mode, tol):
+    """Beam sweep of a formed network against a complex128 product of the same network."""
+    from lyceanem_gb300 import beam_sweep as BS
+    from lyceanem_gb300 import scenes
+    P = _P()
+    s = scenes.sweep_scene(n_side=12, n_clutter=300, n_ground=20, el_n=21, az_n=40, n_beams=37)
+    beta = 2 * np.pi / s.wavelength
+    tris = P.pack_triangles(torch.from_numpy(s.verts), torch.from_numpy(s.faces))
+    g = P.UniformGrid(tris, cell=0.5)
+    G = BS.form_network(s.src, s.pol, s.snk, s.snk_n, beta=beta, grid=g)
+    W = torch.from_numpy(s.weights).cuda()
+    sw = BS.BeamSweep(G, mode)
+    E = sw.fields(sw.run(W)).cpu().numpy()
+    ref = torch.einsum("nmc,kn->mkc", G.cpu().to(torch.complex128), W.cpu().to(torch.complex128)).numpy()
+    err = np.linalg.norm(E - ref) / np.linalg.norm(ref)
+    assert err < tol, err
+    # the network itself against the oracle
+    om = O.Grid(O.pack_triangles(s.verts, s.faces), 0.5).mask(s.src, s.snk, self_to_self=True)
+    Go = O.pair_field(s.src, np.tile(s.pol, (s.src.shape[0], 1)), s.snk, s.snk_n, om, 0.0, beta)
+    assert _pair_rel(G.cpu().numpy(), Go, s.src, s.snk, np.tile(s.pol, (s.src.shape[0], 1)), beta) < FIELD_TOL
