@@ -214,6 +214,31 @@ LYEM_API int lyem_sweep_prepare_weights(const float *d_W, int64_t n_src, int64_t
 LYEM_API int lyem_sweep_run(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
                             const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *stream);
 
+/* --------------------------------------------------------------- adjoint */
+
+/* Reverse-mode derivatives of the direct + one-bounce sink field with the
+ * visibility masks of the forward pass held fixed.  Element n is excited by
+ * a_n e_n (d_src_a complex64 [N], d_src_pol complex64 [N,3]); w_p (complex64
+ * [P,3]) is the scatter-point excitation of the forward pass (sum over
+ * elements of the source->scatter network); masks are the forward stages' bit
+ * masks (d_mask0 sources x sinks, d_mask1 sources x scatter, d_mask2 scatter x
+ * sinks).  Given the cotangent d_grad_E = dL/dE* of a real loss (complex64
+ * [M,3], torch convention) it writes grad a (complex64 [N]), grad x (float
+ * [N,3], element positions) and, if d_grad_y != NULL, grad y (float [M,3],
+ * sink positions); d_scat_z (complex64 [P,3]) receives the back-propagated
+ * field at the scatter points.  Phases are recomputed (FP64 reduction), the
+ * N x M network is not stored.  The forward model is em_wave / ray_launch
+ * (lyceanem/src/em.cuh:18-120) composed as lyceanem/models/frequency_domain.py:195-264
+ * and summed as :847-849; the reference itself has no derivatives.
+ * n_scat = 0 gives the direct path only (scatter pointers may be NULL). */
+LYEM_API size_t lyem_adjoint_workspace(int64_t n_src, int64_t n_scat, int64_t n_snk);
+LYEM_API int lyem_adjoint(const float *d_src_pos, const float *d_src_pol, const float *d_src_a, int64_t n_src,
+                          const float *d_scat_pos, const float *d_scat_nrm, const float *d_scat_w, int64_t n_scat,
+                          const float *d_snk_pos, const float *d_snk_nrm, const float *d_grad_E, int64_t n_snk,
+                          const uint32_t *d_mask0, const uint32_t *d_mask1, const uint32_t *d_mask2, double alpha,
+                          double beta, float *d_grad_a, float *d_grad_x, float *d_grad_y, float *d_scat_z,
+                          void *d_ws, size_t ws_bytes, void *stream);
+
 /* ------------------------------------------ host mirrors of lyceanem.em */
 
 /* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):

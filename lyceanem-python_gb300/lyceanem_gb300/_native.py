@@ -70,6 +70,9 @@ SIGNATURES = {
                                  _f64, _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32,
                                  _vp], ctypes.c_int),
     "lyem_mask_to_bytes": ([_vp, _i64, _i64, _vp, _vp], ctypes.c_int),
+    "lyem_adjoint_workspace": ([_i64, _i64, _i64], _sz),
+    "lyem_adjoint": ([_vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _f64, _f64, _vp,
+                      _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_sweep_network_bytes": ([_i64, _i64, _i32], _sz),
     "lyem_sweep_weights_bytes": ([_i64, _i64, _i32], _sz),
     "lyem_sweep_prepare_network": ([_vp, _i64, _i64, _i32, _i64, _vp, _vp], ctypes.c_int),
