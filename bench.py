@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the mixed-precision beam-sweep measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) measurement")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
     return ap.parse_args()
 
@@ -244,6 +245,8 @@ def run_ours(args, rank, world):
         res["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_sweep:
         res["sweep"] = run_sweep(args)
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        res["adjoint"] = run_adjoint(args)
     if rank == 0 and world == 1 and not args.no_e2e:
         res["e2e"] = run_e2e(args, s, paths)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -348,6 +351,106 @@ def run_sweep(args, n_check=256, reps=5):
     res["speedup_fp16x3_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3"]["ms"]
     res["error_sample"] = f"{n_check} seeded sinks x {K} beams x 3 components, relative Frobenius norm"
     return res
+
+
+# ------------------------------------------------------------------ adjoint
+def _model_fp64(a, x, y, pol, y_n, scat, scat_n, m0, m1, m2, beta, chunk=256):
+    """FP64 torch restatement of the forward sink field (em_wave composed as the reference's one bounce),
+    visibility from the given masks, chunked over scatter points; runs on the GPU in float64."""
+    import numpy as np
+    import torch
+    kappa = 1j * beta
+    front = -1.0 / (2 * np.pi)
+
+    def G(s, e, t, t_n, mask):
+        rv = t[None, :, :] - s[:, None, :]
+        r = torch.sqrt((rv * rv).sum(-1))
+        d = rv / r[..., None]
+        F = front * (-(kappa / r + 1.0 / r ** 2)) * torch.exp(-kappa * r)
+        sd = (t_n[None, :, :] * d).sum(-1)
+        q = e[:, None, :] - (e[:, None, :] * d).sum(-1, keepdim=True) * d
+        return mask[..., None] * (F * sd)[..., None] * q
+
+    E_src = a[:, None] * pol
+    E = G(x, E_src, y, y_n, m0).sum(0)
+    w = G(x, E_src, scat, scat_n, m1).sum(0)
+    for p0 in range(0, scat.shape[0], chunk):
+        p1 = min(p0 + chunk, scat.shape[0])
+        E = E + (w[p0:p1, None, :] * G(scat[p0:p1], w[p0:p1], y, y_n, m2[p0:p1])).sum(0)
+    return E
+
+
+def run_adjoint(args, reps=3):
+    """Differentiation scene: 16x16 array, 10,000 scatter points, 32,761 front-hemisphere sinks; loss
+    sum |E - E_target|^2 with E_target the field of a seeded random-phase excitation.  Times forward and
+    backward and checks gradient components against FP64 central differences (step 1e-4 wavelengths for
+    positions) of an FP64 restatement of the forward model with the same masks."""
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300 import adjoint as A
+    from lyceanem_gb300 import propagation as P
+    from lyceanem_gb300 import scenes
+    s = scenes.adjoint_scene()
+    beta = 2 * np.pi / s.wavelength
+    dev = torch.device("cuda")
+    t = lambda z: torch.from_numpy(np.ascontiguousarray(z)).to(dev)  # noqa: E731
+    tris = P.pack_triangles(t(s.verts), t(s.faces))
+    grid = P.UniformGrid(tris, cell=s.cell)
+    x0, y0, pol = t(s.src), t(s.snk), t(s.E)
+    sn, sc, scn = t(s.snk_n), t(s.scat), t(s.scat_n)
+    kw = dict(beta=beta, grid=grid)
+    with torch.no_grad():
+        target = A.sink_field(t(s.target_excitation), x0, y0, pol, sn, sc, scn, **kw).clone()
+    N, M, Pn = x0.shape[0], y0.shape[0], sc.shape[0]
+    fw, bw = [], []
+    for _ in range(reps + 1):
+        a = torch.ones(N, dtype=torch.complex64, device=dev, requires_grad=True)
+        x = x0.clone().requires_grad_(True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        E = A.sink_field(a, x, y0, pol, sn, sc, scn, **kw)
+        loss = ((E - target).abs() ** 2).sum()
+        e1.record()
+        loss.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        fw.append(e0.elapsed_time(e1))
+        bw.append(e1.elapsed_time(e2))
+    ga, gx = a.grad.detach(), x.grad.detach()
+    # masks of the forward's three stages (deterministic), then FP64 central differences
+    m0 = P.pair_stage(x0, pol, y0, sn, want_mask=True, **kw).mask().double()
+    m1 = P.pair_stage(x0, pol, sc, scn, want_mask=True, **kw).mask().double()
+    m2 = P.pair_stage(sc, pol[:1].expand(Pn, 3), y0, sn, want_mask=True, **kw).mask().double()
+    d64 = lambda z: z.detach().to(torch.float64)  # noqa: E731
+    c64 = lambda z: z.detach().to(torch.complex128)  # noqa: E731
+    args64 = (d64(y0), c64(pol), d64(sn), d64(sc), d64(scn), m0, m1, m2, beta)
+
+    def L(a_, x_):
+        with torch.no_grad():
+            E_ = _model_fp64(a_, x_, args64[0], args64[1], *args64[2:])
+            return float(((E_ - c64(target)).abs() ** 2).sum())
+
+    a64, x64 = torch.ones(N, dtype=torch.complex128, device=dev), d64(x0)
+    h = 1e-4 * s.wavelength
+    rng = np.random.default_rng(11)
+    errs = []
+    for n in rng.choice(N, size=2, replace=False):
+        for part in (1.0, 1j):
+            da = torch.zeros_like(a64)
+            da[n] = part * 1e-4
+            fd = (L(a64 + da, x64) - L(a64 - da, x64)) / 2e-4
+            got = ga[n].real if part == 1.0 else ga[n].imag
+            errs.append(abs(float(got) - fd) / float(ga.abs().max()))
+    for n, k in zip(rng.choice(N, size=2, replace=False), (0, 2)):
+        dx = torch.zeros_like(x64)
+        dx[n, k] = h
+        fd = (L(a64, x64 + dx) - L(a64, x64 - dx)) / (2 * h)
+        errs.append(abs(float(gx[n, k]) - fd) / float(gx.abs().max()))
+    return {"n_elements": N, "n_scatter": Pn, "n_sinks": M, "forward_ms": min(fw[1:]), "backward_ms": min(bw[1:]),
+            "fd_components": len(errs), "fd_max_rel_err": max(errs),
+            "fd_check": "FP64 central differences of an FP64 restatement of the forward with the forward's masks; "
+                        "error = |grad - fd| / max|grad| over 4 excitation and 2 position components"}
 
 
 # ------------------------------------------------------------------ CPU
