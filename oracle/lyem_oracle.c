@@ -17,6 +17,11 @@
  *   - fields are FP64 restatements of the reference formulas, computed from
  *     the same FP32 inputs.
  *
+ * Pinned against the reference itself: tests/test_reference_golden.py
+ * compares this file's masks and fields with outputs of the reference's own
+ * points_to_rays / hit / em_wave run on a GPU (oracle/ref_harness): masks
+ * identical on every pair, fields within the reference's FP32 phase error.
+ *
  * Reference formulas followed (paths within LyceanEM-Python):
  *   ray set-up            lyceanem/src/raycasting.cuh:80-95   (points_to_rays)
  *   ray/triangle test     lyceanem/src/raycasting.cuh:19-68   (hit, back-face cull)

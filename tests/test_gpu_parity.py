@@ -326,3 +326,27 @@ def test_beam_sweep_modes_against_fp64(mode, tol):
     om = O.Grid(O.pack_triangles(s.verts, s.faces), 0.5).mask(s.src, s.snk, self_to_self=True)
     Go = O.pair_field(s.src, np.tile(s.pol, (s.src.shape[0], 1)), s.snk, s.snk_n, om, 0.0, beta)
     assert _pair_rel(G.cpu().numpy(), Go, s.src, s.snk, np.tile(s.pol, (s.src.shape[0], 1)), beta) < FIELD_TOL
+
+
+@pytest.mark.parametrize("case", ["direct", "random"])
+def test_masks_bit_exact_to_reference_device_code(case):
+    """Our brute-force and grid masks against the reference's own hit() run on a GPU
+    (tests/golden/reference_pairs.npz, both builds), and our field against its FP32 field."""
+    import os
+    P = _P()
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_pairs.npz"))
+    g = {x: d[f"{case}_{x}"] for x in ("src", "snk", "snk_n", "verts", "faces", "E", "alpha", "beta", "flag",
+                                       "sample")}
+    N, M = g["src"].shape[0], g["snk"].shape[0]
+    tris = P.pack_triangles(torch.from_numpy(g["verts"]), torch.from_numpy(g["faces"]))
+    kw = dict(beta=float(g["beta"]), alpha=float(g["alpha"]), self_to_self=bool(g["flag"]), want_mask=True,
+              want_pairs=True)
+    for r in (P.pair_stage(g["src"], g["E"], g["snk"], g["snk_n"], tris=tris, **kw),
+              P.pair_stage(g["src"], g["E"], g["snk"], g["snk_n"], grid=P.UniformGrid(tris), **kw)):
+        mask = r.mask().cpu().numpy()
+        for variant in ("fma", "nofma"):
+            ref = np.unpackbits(d[f"{case}_{variant}_vis"])[:N * M].reshape(N, M).astype(bool)
+            assert np.array_equal(mask, ref), f"{int((mask != ref).sum())} pairs differ from the reference"
+        got = r.pairs.cpu().numpy().reshape(-1, 3)[g["sample"]]
+        ref_f = d[f"{case}_fma_field"].astype(np.float32).view(np.complex64).reshape(-1, 3)
+        assert np.abs(got - ref_f).max() / np.abs(ref_f).max() < 1e-3
