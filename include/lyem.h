@@ -239,6 +239,71 @@ LYEM_API int lyem_adjoint(const float *d_src_pos, const float *d_src_pol, const 
                           double beta, float *d_grad_a, float *d_grad_x, float *d_grad_y, float *d_scat_z,
                           void *d_ws, size_t ws_bytes, void *stream);
 
+/* ------------------------------------ many scenes x many frequencies */
+
+/* One scene of a batch: the composition of calculate_scattering_cuda
+ * (lyceanem/models/frequency_domain.py:195-264) summed over the sources
+ * (:847-849), evaluated at every frequency of the batch.  Device pointers.
+ * Scatter points are given in processing order (e.g. lyem_spatial_order);
+ * scat_id[slot] is the caller's index of a slot, used only by the
+ * self_to_self pair-skip rule (NULL: the slot is the index).  The grid is
+ * the scene's uniform grid (lyem_grid_plan / lyem_grid_fill). */
+typedef struct lyem_batch_scene {
+    const float *src_pos;      /* [n_src, 3] */
+    const float *src_E;        /* [n_src, 6] complex excitation (re, im) x (x, y, z) */
+    const float *scat_pos;     /* [n_scat, 3] */
+    const float *scat_nrm;     /* [n_scat, 3] */
+    const int32_t *scat_id;    /* [n_scat] or NULL */
+    const int32_t *cell_start; /* [cells + 1] */
+    const float *cell_tris;    /* [refs, 12], 16-byte aligned */
+    int64_t n_src;
+    int64_t n_scat;
+    float grid_origin[3];
+    float grid_cell;
+    int32_t grid_dims[3];
+    int32_t reserved;
+} lyem_batch_scene;
+
+typedef struct lyem_batch_config {
+    int32_t freq_group;    /* frequencies per thread: 1, 2, 4 or 8; above 1 the beta list must be uniform */
+    int32_t src_chunk;     /* sources per visibility item: 32 or 64 */
+    int32_t blocks_per_sm; /* resident blocks per SM of the persistent launch, 0..8 (0: as many as fit) */
+    int32_t cull;          /* back-face culling (the CUDA engine's rule) */
+    float eps;             /* determinant threshold of the ray-triangle test */
+    int32_t self_to_self;  /* 0: the pair (n, m) with equal indices is not tested (the reference default) */
+    double alpha;          /* attenuation */
+} lyem_batch_config;
+
+/* No counterpart in the reference, which evaluates one scene at one
+ * frequency per call.  All scenes share the sinks (processing order; snk_id
+ * maps a slot to the caller's index, which indexes the output) and the
+ * frequency list beta[n_freq] (rad/m).  Output field[n_scenes][n_freq][n_snk][6]
+ * float (complex64 [S, F, M, 3]):
+ *   E_f(m) = sum_n S0_f(n, m) + sum_p e_p(f) (.) S2_f(p, m; e_p(f)),
+ *   e_p(f) = sum_n S1_f(n, p).
+ * lyem_batch_workspace: bytes of the workspace (0: invalid arguments).
+ * lyem_batch_items: work items of the launch (per kind: three visibility
+ *   stages, scatter fields, sink fields), or minus a status.
+ * lyem_batch_prepare: writes the scene table, the work list and the
+ *   frequency tables into the workspace (256-byte aligned); host -> device
+ *   copies, synchronous with the stream.  Repeat after any change of scenes,
+ *   frequencies or configuration.
+ * lyem_batch_launch: two memsets and one kernel on the stream, nothing else
+ *   (no allocation, no host synchronisation); counters (optional, [n_scenes][4]
+ *   u64: visible pairs of the three stages, ray-triangle tests) are zeroed
+ *   first; blocks_out (optional) receives the persistent grid size. */
+LYEM_API size_t lyem_batch_workspace(const lyem_batch_scene *scenes, int32_t n_scenes, int64_t n_snk,
+                                     int32_t n_freq, const lyem_batch_config *config);
+LYEM_API int64_t lyem_batch_items(const lyem_batch_scene *scenes, int32_t n_scenes, int64_t n_snk, int32_t n_freq,
+                                  const lyem_batch_config *config, int64_t *per_kind5);
+LYEM_API int lyem_batch_prepare(const lyem_batch_scene *scenes, int32_t n_scenes, int64_t n_snk, const double *beta,
+                                int32_t n_freq, const lyem_batch_config *config, void *d_ws, size_t ws_bytes,
+                                void *stream);
+LYEM_API int lyem_batch_launch(const lyem_batch_scene *scenes, int32_t n_scenes, const float *d_snk_pos,
+                               const float *d_snk_nrm, const int32_t *d_snk_id, int64_t n_snk, const double *beta,
+                               int32_t n_freq, const lyem_batch_config *config, void *d_ws, size_t ws_bytes,
+                               float *d_field_out, uint64_t *d_counters, int32_t *blocks_out, void *stream);
+
 /* ------------------------------------------ host mirrors of lyceanem.em */
 
 /* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):

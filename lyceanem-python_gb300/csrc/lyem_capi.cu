@@ -20,7 +20,7 @@ namespace {
 thread_local int g_last_cuda_error = 0;
 
 int cuda_fail(cudaError_t e) {
-    g_last_cuda_error = (int)e;
+    record_cuda_error(e);
     return e == cudaErrorMemoryAllocation ? LYEM_ERR_NOMEM : LYEM_ERR_CUDA;
 }
 
@@ -129,6 +129,8 @@ struct DevBuf {
 };
 
 }  // namespace
+
+void lyem::record_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
 
 extern "C" {
 

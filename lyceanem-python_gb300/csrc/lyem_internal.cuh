@@ -63,6 +63,9 @@ struct StageParams {
     int* snk_visible;              // [n_snk] visible sources per sink (may be nullptr)
 };
 
+// Records the CUDA error that lyem_last_cuda_error() reports (lyem_capi.cu).
+void record_cuda_error(cudaError_t e);
+
 // Host-side count of kernel launches made by this library (lyem_kernel_launches()).
 void note_launches(unsigned long long n);
 unsigned long long launches_so_far();

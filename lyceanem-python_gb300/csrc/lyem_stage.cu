@@ -29,6 +29,7 @@
 
 #include "lyem_device.cuh"
 #include "lyem_internal.cuh"
+#include "lyem_walk.cuh"
 
 namespace lyem {
 
@@ -314,87 +315,6 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
 //             serialised lane by lane.
 // Visibility of the chunk is kept as a 64-bit blocked mask; the field epilogue
 // then runs over the sources in lockstep.
-struct Walk {
-    float ox, oy, oz;
-    Ray r;
-    float ix, iy, iz, t1;
-    int cx, cy, cz, q, q1, guard;
-};
-
-// Starts the walk of segment o -> e; false if the segment misses the grid box.
-__device__ __forceinline__ bool walk_begin(const StageParams& p, Walk& w, float ox, float oy, float oz, float ex,
-                                           float ey, float ez) {
-    w.ox = ox; w.oy = oy; w.oz = oz;
-    w.r = make_ray(ox, oy, oz, ex, ey, ez);
-    float t0 = 0.f;
-    w.t1 = w.r.len;
-    bool miss = false;
-#define LYEM_SLAB(D, O, G0, G1, INV)                       \
-    if (D == 0.f) {                                        \
-        INV = 0.f;                                         \
-        if (O < G0 || O > G1) miss = true;                 \
-    } else {                                               \
-        INV = 1.0f / D;                                    \
-        float ta = (G0 - O) * INV, tb = (G1 - O) * INV;    \
-        t0 = fmaxf(t0, fminf(ta, tb));                     \
-        w.t1 = fminf(w.t1, fmaxf(ta, tb));                 \
-    }
-    LYEM_SLAB(w.r.dx, ox, p.g0[0], p.g1[0], w.ix)
-    LYEM_SLAB(w.r.dy, oy, p.g0[1], p.g1[1], w.iy)
-    LYEM_SLAB(w.r.dz, oz, p.g0[2], p.g1[2], w.iz)
-#undef LYEM_SLAB
-    if (miss || !(t0 <= w.t1)) return false;
-    w.cx = min(max((int)floorf((ox + t0 * w.r.dx - p.g0[0]) * p.inv_cell), 0), p.dims[0] - 1);
-    w.cy = min(max((int)floorf((oy + t0 * w.r.dy - p.g0[1]) * p.inv_cell), 0), p.dims[1] - 1);
-    w.cz = min(max((int)floorf((oz + t0 * w.r.dz - p.g0[2]) * p.inv_cell), 0), p.dims[2] - 1);
-    w.guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
-    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
-    w.q = __ldg(p.cell_start + c);
-    w.q1 = __ldg(p.cell_start + c + 1);
-    return true;
-}
-
-// Tests triangle q of the current cell and advances q; true on a hit.
-template <bool CULL>
-__device__ __forceinline__ bool walk_test(const StageParams& p, Walk& w) {
-    const float4* t = p.cell_tris + 3 * (long long)w.q;
-    const float4 v0 = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
-    ++w.q;
-    return hit_full<CULL>(w.r, w.ox, w.oy, w.oz, v0, e1, e2, p.eps);
-}
-
-// Crosses the nearest cell boundary; false when the segment or the grid ends there.
-__device__ __forceinline__ bool walk_step(const StageParams& p, Walk& w) {
-    const float kInf = __int_as_float(0x7f800000);
-    const float cell = p.cell;
-    const float tx = w.r.dx > 0.f ? (p.g0[0] + (float)(w.cx + 1) * cell - w.ox) * w.ix
-                                  : (w.r.dx < 0.f ? (p.g0[0] + (float)w.cx * cell - w.ox) * w.ix : kInf);
-    const float ty = w.r.dy > 0.f ? (p.g0[1] + (float)(w.cy + 1) * cell - w.oy) * w.iy
-                                  : (w.r.dy < 0.f ? (p.g0[1] + (float)w.cy * cell - w.oy) * w.iy : kInf);
-    const float tz = w.r.dz > 0.f ? (p.g0[2] + (float)(w.cz + 1) * cell - w.oz) * w.iz
-                                  : (w.r.dz < 0.f ? (p.g0[2] + (float)w.cz * cell - w.oz) * w.iz : kInf);
-    bool done;
-    if (tx <= ty && tx <= tz) {
-        w.cx += w.r.dx > 0.f ? 1 : -1;
-        done = tx > w.t1 || w.cx < 0 || w.cx >= p.dims[0];
-    } else if (ty <= tz) {
-        w.cy += w.r.dy > 0.f ? 1 : -1;
-        done = ty > w.t1 || w.cy < 0 || w.cy >= p.dims[1];
-    } else {
-        w.cz += w.r.dz > 0.f ? 1 : -1;
-        done = tz > w.t1 || w.cz < 0 || w.cz >= p.dims[2];
-    }
-    if (--w.guard < 0) {  // a monotone walk visits at most dims[0] + dims[1] + dims[2] cells
-        atomicOr(&g_device_error, 2u);
-        done = true;
-    }
-    if (done) return false;
-    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
-    w.q = __ldg(p.cell_start + c);
-    w.q1 = __ldg(p.cell_start + c + 1);
-    return true;
-}
-
 constexpr int kLockstep = 0;
 constexpr int kRefill = 1;
 
@@ -428,7 +348,7 @@ __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams 
                     ++tests;
                     if (walk_test<CULL>(p, w)) { hit = true; break; }
                 }
-                if (hit || !walk_step(p, w)) break;
+                if (hit || !walk_step(p, w, &g_device_error)) break;
             }
             if (hit) blocked |= 1ull << s;
         }
@@ -460,7 +380,7 @@ __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams 
                         break;
                     }
                 }
-                if (has && !walk_step(p, w)) has = false;
+                if (has && !walk_step(p, w, &g_device_error)) has = false;
             }
         }
     }

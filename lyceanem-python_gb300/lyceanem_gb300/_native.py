@@ -43,6 +43,24 @@ _f32p = ctypes.POINTER(ctypes.c_float)
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
+class BatchScene(ctypes.Structure):
+    """lyem_batch_scene of include/lyem.h (device pointers and sizes of one scene)."""
+    _fields_ = [("src_pos", _vp), ("src_E", _vp), ("scat_pos", _vp), ("scat_nrm", _vp), ("scat_id", _vp),
+                ("cell_start", _vp), ("cell_tris", _vp), ("n_src", _i64), ("n_scat", _i64),
+                ("grid_origin", _f32 * 3), ("grid_cell", _f32), ("grid_dims", _i32 * 3), ("reserved", _i32)]
+
+
+class BatchConfig(ctypes.Structure):
+    """lyem_batch_config of include/lyem.h."""
+    _fields_ = [("freq_group", _i32), ("src_chunk", _i32), ("blocks_per_sm", _i32), ("cull", _i32), ("eps", _f32),
+                ("self_to_self", _i32), ("alpha", _f64)]
+
+
+_scp = ctypes.POINTER(BatchScene)
+_cfgp = ctypes.POINTER(BatchConfig)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
 # argument types of every entry point of include/lyem.h
 SIGNATURES = {
     "lyem_version": ([], ctypes.c_int),
@@ -78,6 +96,11 @@ SIGNATURES = {
     "lyem_sweep_prepare_network": ([_vp, _i64, _i64, _i32, _i64, _vp, _vp], ctypes.c_int),
     "lyem_sweep_prepare_weights": ([_vp, _i64, _i64, _i32, _vp, _vp], ctypes.c_int),
     "lyem_sweep_run": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp], ctypes.c_int),
+    "lyem_batch_workspace": ([_scp, _i32, _i64, _i32, _cfgp], _sz),
+    "lyem_batch_items": ([_scp, _i32, _i64, _i32, _cfgp, _i64p], ctypes.c_int64),
+    "lyem_batch_prepare": ([_scp, _i32, _i64, _f64p, _i32, _cfgp, _vp, _sz, _vp], ctypes.c_int),
+    "lyem_batch_launch": ([_scp, _i32, _vp, _vp, _vp, _i64, _f64p, _i32, _cfgp, _vp, _sz, _vp, _vp, _i32p, _vp],
+                          ctypes.c_int),
     "lyem_em_bin_counts": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp], ctypes.c_int),
     "lyem_em_bin_triangles": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_em_calculate_scattering_brute_force": (
