@@ -358,7 +358,7 @@ def run_sweep(args, n_check=256, reps=5):
 
 
 # ------------------------------------------------------------------ batched
-BATCH_TUNE_CANDIDATES = [(4, 32, 4), (4, 64, 4), (2, 32, 4), (4, 32, 3)]
+BATCH_TUNE_CANDIDATES = [(2, 64, 8), (1, 64, 8), (4, 64, 8), (4, 64, 4)]
 
 
 def run_batched(args, reps=2):

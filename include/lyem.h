@@ -143,10 +143,12 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * sinks share a warp; results are unchanged (sink sums are summed in chunk
  * order, so a different source order can change the last bits of the field).
  * src_chunk: sources per thread block (0 = automatic; at most 32 for brute
- * force, 64 for the grid).  traversal (grid only): 0 = automatic, 1 = all lanes
- * of a warp trace the same source in lockstep, k in 2..33 = each lane moves on
- * to its next source when its ray ends, new rays being started in batches once
- * k-1 lanes of the warp are idle. */
+ * force, 64 for the grid).  traversal (grid only): 1 = all lanes of a warp
+ * trace the same source in lockstep; k in 2..33 = each lane moves on to its
+ * next source when its ray ends, new rays being started in batches once k-1
+ * lanes of the warp are idle; 34, 35, 36 = lockstep with the registers capped
+ * so that 10, 12, 16 blocks fit an SM; 0 = automatic (currently 36).  Every
+ * schedule gives the same results. */
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
                                           int32_t src_chunk);
 LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const float *d_src_W, int64_t n_src,

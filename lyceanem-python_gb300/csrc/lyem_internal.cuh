@@ -52,7 +52,8 @@ struct StageParams {
     // launch shape: blockIdx.y + chunk_base is the source chunk
     int src_chunk;
     long long chunk_base;
-    int refill_lanes;  // grid stage schedule: 0 = lockstep, k > 0 = batched refill once k lanes are idle
+    int refill_lanes;  // grid stage schedule: 0 = lockstep, k > 0 = batched refill once k lanes are idle,
+                       // -10 / -12 / -16 = lockstep with registers capped for that many blocks per SM
     // outputs
     float* partial;              // [n_chunks, n_snk, 6]
     float* pair_out;             // [n_src, n_snk, 6] or nullptr

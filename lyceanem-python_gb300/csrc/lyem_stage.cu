@@ -317,9 +317,17 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
 // then runs over the sources in lockstep.
 constexpr int kLockstep = 0;
 constexpr int kRefill = 1;
+// Lockstep with the registers capped so that 10, 12 or 16 blocks of 128
+// threads fit an SM.  More resident warps hide more of the triangle-load
+// latency: on the 28 GHz one-bounce scene the scatter->sink stage takes 1357 ms
+// uncapped (60 registers, 8 blocks), 1184 / 1067 / 969 ms capped at 10 / 12 /
+// 16 blocks, the last with some spilling; 16 is the default schedule.
+constexpr int kLockstep10 = 2;
+constexpr int kLockstep12 = 3;
+constexpr int kLockstep16 = 4;
 
 template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, int MODE>
-__global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams p) {
+__global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == kLockstep12 ? 12 : MODE == kLockstep16 ? 16 : 1) grid_stage_kernel(const StageParams p) {
     const int tid = threadIdx.x;
     const long long ms = (long long)blockIdx.x * kThreads + tid;
     const bool m_ok = ms < p.n_snk;
@@ -336,7 +344,7 @@ __global__ void __launch_bounds__(kThreads) grid_stage_kernel(const StageParams 
     }
     unsigned long long blocked = 0, tests = 0;
     Walk w;
-    if (MODE == kLockstep) {
+    if (MODE != kRefill) {
         for (int s = 0; s < nsrc; ++s) {
             const long long n = src_index(s);
             if (!m_ok || (p.skip_diag && n == m)) continue;
@@ -422,7 +430,13 @@ static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
         p.chunk_base = base;
         dim3 grid(tiles, (unsigned)(chunks - base < 65535 ? chunks - base : 65535));
         if (p.cell_start) {
-            if (p.refill_lanes > 0)
+            if (p.refill_lanes == -16)
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);
+            else if (p.refill_lanes == -12)
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep12><<<grid, kThreads, 0, stream>>>(p);
+            else if (p.refill_lanes == -10)
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep10><<<grid, kThreads, 0, stream>>>(p);
+            else if (p.refill_lanes > 0)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kRefill><<<grid, kThreads, 0, stream>>>(p);
             else
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep><<<grid, kThreads, 0, stream>>>(p);
