@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) measurement")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched 64-scene x 64-frequency measurement")
+    ap.add_argument("--batched-scenes", type=int, default=64,
+                    help="scenes of the batched measurement (the first S of the 64-scene recipe; profiling cases)")
+    ap.add_argument("--batched-config", default="",
+                    help="fg,chunk,blocks_per_sm for the batched launch instead of the autotuner (profiling cases)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
     return ap.parse_args()
 
@@ -375,16 +379,21 @@ def run_batched(args, reps=2):
     from lyceanem_gb300 import propagation as P
     from lyceanem_gb300 import scenes as SC
     from oracle import oracle as O
-    scenes, snk, snk_n, freqs = SC.batched_scenes()
+    scenes, snk, snk_n, freqs = SC.batched_scenes(n_scenes=args.batched_scenes)
     t0 = time.time()
     bs = B.BatchedScattering(scenes, snk, snk_n, freqs)
     torch.cuda.synchronize()
     setup_s = time.time() - t0
     t0 = time.time()
-    proxy = B.BatchedScattering([scenes[i] for i in B.stratified_subset(scenes, snk.shape[0])], snk, snk_n, freqs)
-    tune = bs.autotune(candidates=BATCH_TUNE_CANDIDATES, proxy=proxy, use_cache=False)
-    del proxy
-    torch.cuda.empty_cache()
+    if args.batched_config:
+        bs.configure(tuple(int(v) for v in args.batched_config.split(",")))
+        tune = {}
+    else:
+        proxy = B.BatchedScattering([scenes[i] for i in B.stratified_subset(scenes, snk.shape[0])], snk, snk_n,
+                                    freqs)
+        tune = bs.autotune(candidates=BATCH_TUNE_CANDIDATES, proxy=proxy, use_cache=False)
+        del proxy
+        torch.cuda.empty_cache()
     tune_s = time.time() - t0
     bs.capture()
     bs.run()
