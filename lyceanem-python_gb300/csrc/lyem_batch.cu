@@ -10,20 +10,22 @@
 // beta_f and the visibility of raycasting.cuh:19-95, which is the same for
 // every frequency and is therefore resolved once.
 //
-// Work is a queue of items that a fixed set of resident blocks takes in order:
-//   V items  visibility of one source chunk (32 or 64 sources) against a tile
-//            of 256 sinks, for one of the three stages of a scene (sources ->
+// Work is a queue of items that the warps of a fixed set of resident blocks
+// take in order, each warp on its own (no block-wide barrier: a warp whose
+// rays end early moves on instead of waiting for the slowest warp of a tile):
+//   V items  visibility of one source chunk (32 or 64 sources) against 32
+//            sinks, for one of the three stages of a scene (sources ->
 //            scatter points, sources -> sinks, scatter points -> sinks): grid
 //            DDA, all lanes on the same source at a time; each lane stores
 //            its sink's visibility of the chunk as bits of a sink-major mask
 //            (one 32-bit word per 32 sources);
-//   W items  e_p(f) for a tile of scatter points and every frequency;
-//   E items  E_f(m) for a tile of sinks and every frequency.
+//   W items  e_p(f) for a run of (scatter point, frequency group) slots;
+//   E items  E_f(m) for a run of (sink, frequency group) slots.
 // The queue holds every V item, then every W item, then every E item.  A W
 // item needs its scene's sources -> scatter visibility; an E item needs the
 // two other visibility stages and all W items of its scene.  They wait on the
 // scene's completion counters.  Every item waited on was taken from the queue
-// earlier by a running block that itself waits only on items taken before it,
+// earlier by a running warp that itself waits only on items taken before it,
 // so each wait ends; the waits are bounded all the same and raise bit 0 of
 // the error word on expiry.
 //
@@ -52,8 +54,9 @@
 namespace lyem {
 namespace {
 
-constexpr int kBT = 256;  // threads per block; also the sinks of a visibility tile
-constexpr long long kItemPairs = 1LL << 16;  // candidate pairs a field item should cover at least
+constexpr int kBT = 256;  // threads per block (8 independent warps)
+constexpr int kWarpSinks = 32;               // sinks of a visibility item (one per lane)
+constexpr long long kItemPairs = 1LL << 14;  // candidate pairs a field item should cover at least
 constexpr int kKinds = 5;
 enum Kind { kVisScat = 0, kVisDirect = 1, kVisBounce = 2, kFieldW = 3, kFieldE = 4 };
 
@@ -97,8 +100,7 @@ struct BatchParams {
     const float* beta_f;    // [n_freq] beta rounded to FP32
     float2 dbeta_ff;        // uniform frequency step of beta as float-float
     int n_freq;
-    int n_groups;           // ceil(n_freq / FG)
-    int tile_sinks;         // sinks of a field item = kBT / n_groups
+    int n_groups;           // ceil(n_freq / FG); a field slot is (point, group), slot = point * n_groups + group
     int src_chunk;
     float alpha;
     int skip_diag;
@@ -173,10 +175,10 @@ __device__ bool wait_count(const unsigned* ctr, unsigned target) {
     }
 }
 
-__device__ bool wait_deps(const BatchParams& P, const int4& it) {
-    const DevScene& S = P.scenes[it.y];
-    const unsigned* d = P.done + (long long)it.y * kKinds;
-    if (it.x == kFieldW) return wait_count(d + kVisScat, (unsigned)S.expect[kVisScat]);
+__device__ bool wait_deps(const BatchParams& P, int kind, int scene) {
+    const DevScene& S = P.scenes[scene];
+    const unsigned* d = P.done + (long long)scene * kKinds;
+    if (kind == kFieldW) return wait_count(d + kVisScat, (unsigned)S.expect[kVisScat]);
     bool ok = wait_count(d + kVisDirect, (unsigned)S.expect[kVisDirect]);
     ok = ok && wait_count(d + kVisBounce, (unsigned)S.expect[kVisBounce]);
     ok = ok && wait_count(d + kFieldW, (unsigned)S.expect[kFieldW]);
@@ -195,15 +197,15 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 // the caller) rather than held in registers through the walk.
 template <bool CULL>
 __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView& G, int scene, int stage,
-                         long long n0, long long tile0) {
-    const int tid = threadIdx.x;
+                         long long n0, long long m0) {
+    const int lane = threadIdx.x & 31;
     const float* spos = stage == kVisBounce ? S.scat_pos : S.src_pos;
     const long long ns = stage == kVisBounce ? S.n_scat : S.n_src;
     const int* sid = stage == kVisBounce ? S.scat_id : nullptr;
     const float* kpos = stage == kVisScat ? S.scat_pos : P.snk_pos;
     const long long nk = stage == kVisScat ? S.n_scat : P.n_snk;
     const int* kid = stage == kVisScat ? S.scat_id : P.snk_id;
-    const long long ms = tile0 + tid;
+    const long long ms = m0 + lane;
     const bool ok = ms < nk;
     const long long rem = ns - n0;
     const int nsrc = (int)(rem < P.src_chunk ? rem : P.src_chunk);
@@ -251,7 +253,7 @@ __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView
     if (P.counters) {
         const unsigned long long v = warp_sum((unsigned long long)__popcll(vis));
         const unsigned long long t = warp_sum(tests);
-        if ((tid & 31) == 0) {
+        if (lane == 0) {
             atomicAdd(P.counters + 4LL * scene + stage, v);
             atomicAdd(P.counters + 4LL * scene + 3, t);
         }
@@ -370,18 +372,20 @@ __device__ __forceinline__ void field_stage(const BatchParams& P, const unsigned
     }
 }
 
+// One warp's 32 consecutive slots (chunk of the scene's slot list).
 template <int FG>
-__device__ void field_item(const BatchParams& P, const DevScene& S, int scene, int kind, long long tile0,
+__device__ void field_item(const BatchParams& P, const DevScene& S, int scene, int kind, long long chunk,
                            float* sacc) {
     const int tid = threadIdx.x;
     const int G = P.n_groups;
-    const int sub = tid / G, g = tid - sub * G;
-    const long long ms = tile0 + sub;
     const bool at_sinks = kind == kFieldE;
     const long long nk = at_sinks ? P.n_snk : S.n_scat;
+    const long long slot = chunk * 32 + (tid & 31);
+    const long long ms = slot / G;
+    const int g = (int)(slot - ms * G);
     const int f0 = g * FG;
     const int cnt = min(FG, P.n_freq - f0);
-    const bool ok = sub < P.tile_sinks && ms < nk && cnt > 0;
+    const bool ok = ms < nk && cnt > 0;
 #pragma unroll
     for (int k = 0; k < 6 * FG; ++k) sacc[k * kBT + tid] = 0.f;
     float ex = 0.f, ey = 0.f, ez = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
@@ -426,51 +430,56 @@ __device__ void field_item(const BatchParams& P, const DevScene& S, int scene, i
 // ---------------------------------------------------------------- kernel
 
 // MINB: blocks per SM the register allocation is capped for (1: uncapped).
-// Thread 0 takes the next queue position while the block works on the
-// current item, so the atomic's latency is hidden; a block therefore holds
-// one taken-but-unstarted item.  Progress still holds: the smallest
+// Each warp works on its own: lane 0 takes the next queue position while the
+// warp works on the current item (the atomic's latency is hidden), so a warp
+// holds one taken-but-unstarted item.  Progress still holds: the smallest
 // unfinished queue position is always being worked on (its holder took it
 // after every item it could be busy with), and it waits only on smaller
 // positions, which are finished.
 template <bool CULL, int FG, int MINB>
 __global__ void __launch_bounds__(kBT, MINB) batch_kernel(const BatchParams P) {
     extern __shared__ float sacc[];
-    __shared__ int4 s_item;
-    __shared__ int s_run;
-    __shared__ GridView s_grid;
+    __shared__ GridView s_grid[kBT / 32];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned nxt = 0;
-    if (threadIdx.x == 0) nxt = atomicAdd(P.head, 1u);
+    if (lane == 0) nxt = atomicAdd(P.head, 1u);
     while (true) {
-        if (threadIdx.x == 0) {
+        int kind = -1, scene = 0, a = 0, b = 0, run = 1;
+        if (lane == 0) {
             const unsigned i = nxt;
-            int4 it = make_int4(-1, 0, 0, 0);
             if (i < (unsigned)P.n_items) {
-                it = P.items[i];
+                const int4 it = P.items[i];
+                kind = it.x;
+                scene = it.y;
+                a = it.z;
+                b = it.w;
                 nxt = atomicAdd(P.head, 1u);
+                if (kind >= kFieldW && !wait_deps(P, kind, scene)) {
+                    atomicOr(P.err, 1u);
+                    run = 0;  // the item is skipped; its outputs are not valid
+                }
+                if (kind < kFieldW) s_grid[wid] = P.scenes[scene].grid;
             }
-            int run = 1;
-            if (it.x >= kFieldW && !wait_deps(P, it)) {
-                atomicOr(P.err, 1u);
-                run = 0;  // the item is skipped; its outputs are not valid
-            }
-            s_item = it;
-            s_run = run;
-            if (it.x >= 0 && it.x < kFieldW) s_grid = P.scenes[it.y].grid;
         }
-        __syncthreads();
-        const int4 it = s_item;
-        if (it.x < 0) break;
-        if (s_run) {
-            const DevScene& S = P.scenes[it.y];
-            if (it.x < kFieldW)
-                vis_item<CULL>(P, S, s_grid, it.y, it.x, (long long)it.z, (long long)it.w);
+        kind = __shfl_sync(full, kind, 0);
+        scene = __shfl_sync(full, scene, 0);
+        a = __shfl_sync(full, a, 0);
+        b = __shfl_sync(full, b, 0);
+        run = __shfl_sync(full, run, 0);
+        __syncwarp();  // s_grid[wid] is visible to the warp
+        if (kind < 0) break;
+        if (run) {
+            const DevScene& S = P.scenes[scene];
+            if (kind < kFieldW)
+                vis_item<CULL>(P, S, s_grid[wid], scene, kind, (long long)a, (long long)b);
             else
-                for (int t = 0; t < it.w; ++t)  // it.w consecutive tiles
-                    field_item<FG>(P, S, it.y, it.x, (long long)it.z + (long long)t * P.tile_sinks, sacc);
+                for (int t = 0; t < b; ++t)  // b consecutive 32-slot chunks
+                    field_item<FG>(P, S, scene, kind, (long long)a + t, sacc);
         }
         __threadfence();
-        __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(P.done + (long long)it.y * kKinds + it.x, 1u);
+        __syncwarp();
+        if (lane == 0) atomicAdd(P.done + (long long)scene * kKinds + kind, 1u);
     }
 }
 
@@ -500,9 +509,8 @@ int make_plan(const lyem_batch_scene* sc, int n_scenes, long long n_snk, int n_f
     if (!sc || n_scenes <= 0 || n_snk <= 0 || n_freq <= 0 || !config_ok(cfg)) return LYEM_ERR_INVALID;
     if (n_snk >= (1LL << 31) || n_freq > 4096) return LYEM_ERR_OVERFLOW;
     const int FG = cfg->freq_group;
-    const int groups = (n_freq + FG - 1) / FG;
-    if (groups > kBT) return LYEM_ERR_INVALID;  // a field item needs one thread per frequency group
-    const int tile_f = kBT / groups;
+    const long long groups = (n_freq + FG - 1) / FG;
+    if ((n_snk * groups + 31) / 32 >= (1LL << 31)) return LYEM_ERR_OVERFLOW;  // 32-slot chunk index in an int
     const long long chunk = cfg->src_chunk;
     size_t off = 0;
     pl.off_ctrl = off;
@@ -533,6 +541,7 @@ int make_plan(const lyem_batch_scene* sc, int n_scenes, long long n_snk, int n_f
             nc *= sc[s].grid_dims[k];
         }
         if (!(sc[s].grid_cell > 0.f) || !isfinite(sc[s].grid_cell) || nc >= (1LL << 30)) return LYEM_ERR_INVALID;
+        if ((P * groups + 31) / 32 >= (1LL << 31)) return LYEM_ERR_OVERFLOW;
         cost[s] = (double)N * (double)n_snk + (double)N * (double)P + (double)P * (double)n_snk;
         order[s] = s;
     }
@@ -552,9 +561,9 @@ int make_plan(const lyem_batch_scene* sc, int n_scenes, long long n_snk, int n_f
     pl.items.clear();
     auto add_vis = [&](int s, int stage, long long ns, long long nk) {
         for (long long n0 = 0; n0 < ns; n0 += chunk)
-            for (long long t = 0; t < nk; t += kBT) pl.items.push_back(make_int4(stage, s, (int)n0, (int)t));
+            for (long long t = 0; t < nk; t += kWarpSinks) pl.items.push_back(make_int4(stage, s, (int)n0, (int)t));
         pl.expect[(size_t)s * kKinds + stage] =
-            (int)(((ns + chunk - 1) / chunk) * ((nk + kBT - 1) / kBT));
+            (int)(((ns + chunk - 1) / chunk) * ((nk + kWarpSinks - 1) / kWarpSinks));
     };
     for (int s : order) {
         const long long N = sc[s].n_src, P = sc[s].n_scat;
@@ -562,16 +571,16 @@ int make_plan(const lyem_batch_scene* sc, int n_scenes, long long n_snk, int n_f
         add_vis(s, kVisDirect, N, n_snk);
         add_vis(s, kVisBounce, P, n_snk);
     }
-    // Field items span enough consecutive tiles for about kItemPairs candidate
-    // pairs, so that scenes with few sources do not become thousands of tiny items.
+    // A field item is a run of 32-slot chunks (slot = point * groups + group),
+    // long enough for about kItemPairs candidate (pair, group) evaluations, so
+    // that scenes with few sources do not become very many tiny items.
     auto add_field = [&](int s, int kind, long long nk, long long pairs_per_sink) {
-        const long long per_tile = std::max(1LL, pairs_per_sink * tile_f);
-        const long long k = std::min(64LL, std::max(1LL, (kItemPairs + per_tile - 1) / per_tile));
-        const long long span = k * tile_f;
+        const long long chunks = (nk * groups + 31) / 32;
+        const long long per_chunk = std::max(1LL, pairs_per_sink * 32 / groups);
+        const long long k = std::min(64LL, std::max(1LL, (kItemPairs + per_chunk - 1) / per_chunk));
         int count = 0;
-        for (long long t = 0; t < nk; t += span) {
-            const long long tiles = std::min(k, (nk - t + tile_f - 1) / tile_f);
-            pl.items.push_back(make_int4(kind, s, (int)t, (int)tiles));
+        for (long long c = 0; c < chunks; c += k) {
+            pl.items.push_back(make_int4(kind, s, (int)c, (int)std::min(k, chunks - c)));
             ++count;
         }
         pl.expect[(size_t)s * kKinds + kind] = count;
@@ -780,7 +789,6 @@ LYEM_API int lyem_batch_launch(const lyem_batch_scene* scenes, int32_t n_scenes,
     P.dbeta_ff = step;
     P.n_freq = n_freq;
     P.n_groups = (n_freq + config->freq_group - 1) / config->freq_group;
-    P.tile_sinks = kBT / P.n_groups;
     P.src_chunk = config->src_chunk;
     P.alpha = (float)config->alpha;
     P.skip_diag = config->self_to_self ? 0 : 1;

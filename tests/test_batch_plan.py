@@ -41,16 +41,19 @@ def test_item_counts(fg, chunk):
     cfg = _cfg(fg, chunk)
     per = (ctypes.c_int64 * 5)()
     n = lib.lyem_batch_items(scenes, 3, M, F, ctypes.byref(cfg), per)
-    tile = 256 // _ceil(F, fg)
+    groups = _ceil(F, fg)
 
     def field_items(nk, pairs_per_sink):
-        # a field item spans k consecutive tiles, k = ceil(2^16 / candidate pairs of a tile), 1..64
-        k = min(64, max(1, _ceil(1 << 16, max(1, pairs_per_sink * tile))))
-        return _ceil(nk, k * tile)
+        # a field item is a run of k 32-slot chunks (slot = point * groups + group),
+        # k = ceil(2^14 / candidate pairs of a chunk), 1..64
+        chunks = _ceil(nk * groups, 32)
+        k = min(64, max(1, _ceil(1 << 14, max(1, pairs_per_sink * 32 // groups))))
+        return _ceil(chunks, k)
 
-    vis = [sum(_ceil(N, chunk) * _ceil(Pn, 256) for N, Pn in sizes),
-           sum(_ceil(N, chunk) * _ceil(M, 256) for N, _ in sizes),
-           sum(_ceil(Pn, chunk) * _ceil(M, 256) for _, Pn in sizes)]
+    # visibility items: one source chunk x 32 sinks (one warp)
+    vis = [sum(_ceil(N, chunk) * _ceil(Pn, 32) for N, Pn in sizes),
+           sum(_ceil(N, chunk) * _ceil(M, 32) for N, _ in sizes),
+           sum(_ceil(Pn, chunk) * _ceil(M, 32) for _, Pn in sizes)]
     expect = vis + [sum(field_items(Pn, N) for N, Pn in sizes), sum(field_items(M, N + Pn) for N, Pn in sizes)]
     assert list(per) == expect
     assert n == sum(expect)
@@ -65,9 +68,9 @@ def test_rejects_bad_arguments():
     scenes = (BatchScene * 1)(_scene(64, 10))
     for cfg in (_cfg(fg=3), _cfg(chunk=48), _cfg(bps=9)):
         assert lib.lyem_batch_workspace(scenes, 1, 100, 16, ctypes.byref(cfg)) == 0
-    # one thread per frequency group: more than 256 groups do not fit a block
-    assert lib.lyem_batch_workspace(scenes, 1, 100, 300, ctypes.byref(_cfg(fg=1))) == 0
-    assert lib.lyem_batch_workspace(scenes, 1, 100, 300, ctypes.byref(_cfg(fg=2))) > 0
+    # any number of frequency groups (slots of 32 (point, group) pairs per warp); at most 4,096 frequencies
+    assert lib.lyem_batch_workspace(scenes, 1, 100, 300, ctypes.byref(_cfg(fg=1))) > 0
+    assert lib.lyem_batch_workspace(scenes, 1, 100, 5000, ctypes.byref(_cfg(fg=2))) == 0
     bad = (BatchScene * 1)(_scene(64, 10))
     bad[0].cell_start = None
     assert lib.lyem_batch_workspace(bad, 1, 100, 16, ctypes.byref(_cfg())) == 0
