@@ -306,6 +306,28 @@ LYEM_API int lyem_batch_launch(const lyem_batch_scene *scenes, int32_t n_scenes,
                                int32_t n_freq, const lyem_batch_config *config, void *d_ws, size_t ws_bytes,
                                float *d_field_out, uint64_t *d_counters, int32_t *blocks_out, void *stream);
 
+/* ------------------------------------------------ numba-engine products */
+
+/* f <- f - (f . n^) n^ for complex 3-vectors d_vec [n,6] and vectors d_normals [n,3]
+ * (n^ = n/|n|; a zero n leaves f unchanged): the tangential projection of
+ * sourcelaunchtransformGPU (lyceanem/electromagnetics/empropagation.py:179-258). */
+LYEM_API int lyem_tangential_project(float *d_vec, const float *d_normals, int64_t n, void *stream);
+
+/* Field of every path row of the numba engine, summed per (source, sink):
+ * freqdomainkernal (lyceanem/electromagnetics/empropagation.py:1083-1265) over
+ * the index of workchunkingv2 (lyceanem/raycasting/rayfunctions.py:2681-2955).
+ * d_paths [n_paths, n_cols] int32, 1-based indices into the point arrays
+ * (sources 1..n_src, sinks n_src+1..n_src+n_snk, then scatter points; 0 = none);
+ * d_pos, d_nrm [n_pts,3]; d_w [n_pts,6] complex weights (the sources' field,
+ * factors at later points); d_magnetic [n_pts] (NULL: all electric) with
+ * d_impedance [n_pts] (sqrt(mu/eps)).  Adds to d_out [n_src, n_snk, 3, 2]
+ * double (complex128 [n_src, n_snk, 3]; the caller zeroes it).  Rows with an
+ * index out of range set device error bit 1 and are skipped. */
+LYEM_API int lyem_path_field(const int32_t *d_paths, int64_t n_paths, int32_t n_cols, const float *d_pos,
+                             const float *d_nrm, const float *d_w, const uint8_t *d_magnetic,
+                             const float *d_impedance, int64_t n_pts, int64_t n_src, int64_t n_snk, double alpha,
+                             double beta, double *d_out, void *stream);
+
 /* ------------------------------------------ host mirrors of lyceanem.em */
 
 /* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):

@@ -1,0 +1,74 @@
+"""Numba-engine field products with the call shape of lyceanem/electromagnetics/empropagation.py.
+
+EMGPUFreqDomain evaluates every path row of the numba engine's index (see
+raycasting.workchunkingv2) on the GPU (lyem_path_field) and sums the fields
+per (source, sink), as freqdomainkernal does
+(lyceanem/electromagnetics/empropagation.py:1083-1265, 2197-2410).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import propagation as P
+from ._native import LyemError, check, lib
+
+# scattering_point of lyceanem/base_types.py (numpy record layout, no numba needed)
+scattering_point = np.dtype([("px", "f4"), ("py", "f4"), ("pz", "f4"), ("vx", "f4"), ("vy", "f4"), ("vz", "f4"),
+                             ("nx", "f4"), ("ny", "f4"), ("nz", "f4"), ("ex", "c8"), ("ey", "c8"), ("ez", "c8"),
+                             ("permittivity", "c8"), ("permeability", "c8"), ("Electric", "?")], align=True)
+
+
+def _vp(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def path_network(full_index, pos, nrm, weights, n_src, n_snk, alpha, beta, magnetic=None, impedance=None):
+    """complex128 [n_src, n_snk, 3] on the device: the path rows' fields summed per (source, sink)."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    idx = torch.as_tensor(np.ascontiguousarray(np.asarray(full_index), dtype=np.int32), device=dev)
+    pos = P._points(pos)
+    nrm = P._points(nrm)
+    w = torch.view_as_real(P._cvec(weights, pos.shape[0])).reshape(-1, 6).contiguous()
+    mag = imp = None
+    if magnetic is not None and np.any(np.asarray(magnetic)):
+        mag = torch.as_tensor(np.asarray(magnetic, dtype=np.uint8), device=dev)
+        imp = torch.as_tensor(np.asarray(impedance, dtype=np.float32), device=dev)
+    out = torch.zeros((n_src, n_snk, 3, 2), dtype=torch.float64, device=dev)
+    rows, cols = (idx.shape[0], idx.shape[1]) if idx.dim() == 2 else (0, 2)
+    check(lib.lyem_path_field(_vp(idx), rows, cols, _vp(pos), _vp(nrm), _vp(w), _vp(mag), _vp(imp), pos.shape[0],
+                              n_src, n_snk, float(alpha), float(beta), _vp(out), P._stream()), "path_field")
+    st, flags = P.device_errors()
+    if st != 0 or flags != 0:
+        raise LyemError(st or 1, f"path_field: device error word {flags:#x} (an index out of range)")
+    return torch.view_as_complex(out)
+
+
+def EMGPUFreqDomain(source_num, sink_num, full_index, point_information, wavelength, alpha, beta):
+    """Scattering network complex128 [source_num, sink_num, 3] of the paths in full_index
+    (lyceanem/electromagnetics/empropagation.py:2197-2410); point_information is an array
+    of scattering_point records ([sources, sinks, scatter points])."""
+    del wavelength  # the reference's kernel takes alpha and beta; wavelength is unused there
+    pts = np.asarray(point_information)
+    pos = np.stack([pts["px"], pts["py"], pts["pz"]], 1).astype(np.float32)
+    nrm = np.stack([pts["nx"], pts["ny"], pts["nz"]], 1).astype(np.float32)
+    w = np.stack([pts["ex"], pts["ey"], pts["ez"]], 1).astype(np.complex64)
+    magnetic = impedance = None
+    if "Electric" in pts.dtype.names and not np.all(pts["Electric"]):
+        magnetic = ~pts["Electric"].astype(bool)
+        impedance = np.sqrt(np.real(pts["permeability"]).astype(np.float64)
+                            / np.real(pts["permittivity"]).astype(np.float64)).astype(np.float32)
+    idx = np.asarray(full_index)
+    if idx.size == 0:
+        return np.zeros((source_num, sink_num, 3), np.complex128)
+    net = path_network(idx, pos, nrm, w, int(source_num), int(sink_num), alpha, beta, magnetic, impedance)
+    return net.cpu().numpy()
+
+
+def tangential_project(vec, normals):
+    """In place on a complex64 [n, 3] CUDA tensor: f - (f . n^) n^ (sourcelaunchtransformGPU
+    with a surface normal, lyceanem/electromagnetics/empropagation.py:179-258)."""
+    nrm = P._points(normals)
+    v = torch.view_as_real(vec)
+    check(lib.lyem_tangential_project(_vp(v), _vp(nrm), vec.shape[0], P._stream()), "tangential_project")
+    return vec

@@ -217,3 +217,150 @@ def farfield_theta_phi(E, theta, phi):
     et = Ex * np.cos(phi) * np.cos(theta) + Ey * np.sin(phi) * np.cos(theta) - Ez * np.sin(theta)
     ep = -Ex * np.sin(phi) + Ey * np.cos(phi)
     return et, ep
+
+
+# ---------------------------------------------------------------- numba engine
+# Restatement of the numba engine's path list and per-path product (test
+# infrastructure).  The engine itself cannot run here (numba and cupy are not
+# installed), so these follow its source:
+#   path index   workchunkingv2 / create_model_index / rayHits1Dv2
+#                (lyceanem/raycasting/rayfunctions.py:2624-2955, 1845-1878)
+#   path product freqdomainkernal / sourcelaunchtransformGPU / lossy_propagation
+#                (lyceanem/electromagnetics/empropagation.py:1083-1265, 179-258, 769-801)
+#   visibility   hit without back-face culling, EPSILON 1e-7 (rayfunctions.py:19, 37-104),
+#                every pair tested (create_model_index drops only index-equal end points).
+
+NUMBA_EPSILON = np.float32(1e-7)
+
+
+def numba_masks(src, snk, scat, tris12):
+    """Visibility of the numba engine's three ray sets: (sources->sinks, sources->scatter,
+    scatter->sinks, scatter->scatter), bool arrays."""
+    kw = dict(self_to_self=True, cull=False, eps=NUMBA_EPSILON)
+    P = _f3(scat).shape[0]
+    m0 = mask_brute(src, snk, tris12, **kw)
+    m1 = mask_brute(src, scat, tris12, **kw) if P else np.zeros((_f3(src).shape[0], 0), bool)
+    m2 = mask_brute(scat, snk, tris12, **kw) if P else np.zeros((0, _f3(snk).shape[0]), bool)
+    m3 = mask_brute(scat, scat, tris12, **kw) if P else np.zeros((0, 0), bool)
+    return m0, m1, m2, m3
+
+
+def numba_path_index(N, M, P, m0, m1, m2, m3, max_scatter, line_of_sight=True):
+    """full_index and RAYS_CAST of workchunkingv2 (unchunked ordering for max_scatter 1 and 2;
+    the source-chunked ordering of max_scatter 3).  Indices are 1-based into
+    [sources, sinks, scatter points]."""
+    snk0, sc0 = N + 1, N + M + 1
+    if max_scatter == 1:
+        n, m = np.nonzero(m0)
+        return np.stack([n + 1, m + snk0], 1).astype(np.int32), N * (M + P)
+    if max_scatter == 2:
+        rows = []
+        if line_of_sight:
+            n, m = np.nonzero(m0)
+            rows.append(np.stack([n + 1, m + snk0, np.zeros_like(n)], 1))
+        n1, p1 = np.nonzero(m1)
+        k, m = np.nonzero(m2[p1])
+        rows.append(np.stack([n1[k] + 1, p1[k] + sc0, m + snk0], 1))
+        rays = N * ((M if line_of_sight else 0) + P) + n1.size * M
+        return np.concatenate(rows, 0).astype(np.int32).reshape(-1, 3), rays
+    if max_scatter != 3:
+        raise ValueError("max_scatter must be 1, 2 or 3")
+    ray_estimate = N * (M + P) + N * (P * M * max_scatter)
+    chunknum = max(2, min(N, int(np.ceil(ray_estimate / 2e8))))
+    bounds = np.linspace(0, N, chunknum, dtype=np.int32)
+    out = []
+    rays = 0
+    for c in range(bounds.size - 1):
+        s0, s1 = int(bounds[c]), int(bounds[c + 1])
+        rows = []
+        if line_of_sight:
+            n, m = np.nonzero(m0[s0:s1])
+            rows.append(np.stack([n + s0 + 1, m + snk0, np.zeros_like(n), np.zeros_like(n)], 1))
+        n1, p1 = np.nonzero(m1[s0:s1])
+        n1 = n1 + s0
+        # second wave: each (n, p) to every sink, then every scatter point q != p
+        k, m = np.nonzero(m2[p1])
+        rows.append(np.stack([n1[k] + 1, p1[k] + sc0, m + snk0, np.zeros_like(k)], 1))
+        vis_q = m3[p1].copy()
+        vis_q[np.arange(p1.size), p1] = False
+        k2, q = np.nonzero(vis_q)
+        # third wave: each (n, p, q) to every sink
+        k3, m3_ = np.nonzero(m2[q])
+        rows.append(np.stack([n1[k2][k3] + 1, p1[k2][k3] + sc0, q[k3] + sc0, m3_ + snk0], 1))
+        out.append(np.concatenate(rows, 0))
+        first = (s1 - s0) * ((M if line_of_sight else 0) + P)
+        rays = first + n1.size * (M + P - 1) + k2.size * M  # the reference keeps the last chunk's count
+    return np.concatenate(out, 0).astype(np.int32).reshape(-1, 4), rays
+
+
+def _proj(f, x):
+    """f - (f . x^) x^ for complex f (..., 3) and real x (..., 3)."""
+    u = x / np.linalg.norm(x, axis=-1, keepdims=True)
+    return f - np.sum(f * u, axis=-1, keepdims=True) * u
+
+
+def _seg_loss(a, b, nb, alpha, beta):
+    d = b - a
+    r = np.linalg.norm(d, axis=-1)
+    dn = d / r[:, None]
+    G = np.exp(-(alpha + 1j * beta) * r) / r
+    dG = (-(alpha + 1j * beta) - 1.0 / r) * G
+    return -(1.0 / (2 * np.pi)) * dG * np.sum(dn * nb, axis=-1), dn
+
+
+def path_field(full_index, pos, nrm, w, n_src, n_snk, alpha, beta, magnetic=None, impedance=None):
+    """FP64 per-path product of freqdomainkernal summed per (source, sink): complex128 (N, M, 3).
+    A zero index read as a point is the last point (Python's -1), as in the reference."""
+    idx = np.asarray(full_index, dtype=np.int64)
+    pos = np.asarray(pos, np.float32).astype(np.float64)
+    nrm = np.asarray(nrm, np.float32).astype(np.float64)
+    w = np.asarray(w).astype(np.complex128)
+    npt = pos.shape[0]
+    pt = np.where(idx > 0, idx - 1, npt - 1)
+    R, K = idx.shape
+    a0, a1 = pt[:, 0], pt[:, 1]
+    f = w[a0].copy()
+    if magnetic is not None and np.any(magnetic[a0]):
+        sel = np.asarray(magnetic, bool)[a0]
+        d = pos[a1] - pos[a0]
+        d /= np.linalg.norm(d, axis=-1, keepdims=True)
+        f[sel] = np.cross(w[a0][sel], d[sel]) / np.asarray(impedance, np.float64)[a0][sel][:, None]
+    loss = np.ones(R, np.complex128)
+    for i in range(K - 1):
+        ai = pt[:, i]
+        if i > 0:
+            f = _proj(f, nrm[ai])
+        has = idx[:, i + 1] != 0
+        if np.any(has):
+            b = pt[has, i + 1]
+            L, dn = _seg_loss(pos[ai[has]], pos[b], nrm[b], alpha, beta)
+            f[has] = _proj(f[has], dn) * w[b]
+            loss[has] *= L
+    f *= loss[:, None]
+    last = np.zeros(R, np.int64)
+    for i in range(K):
+        last = np.where(idx[:, i] != 0, idx[:, i], last)
+    out = np.zeros((n_src, n_snk, 3), np.complex128)
+    np.add.at(out, (idx[:, 0] - 1, last - n_src - 1), f)
+    return out
+
+
+def numba_sink_field(src, srcE, snk, snk_nrm, scat, scat_nrm, alpha, beta, masks, scattering, los=True):
+    """FP64 sink field of the numba engine for scattering 0 or 1 in factored form:
+      scattering 0:  sum_n S0[n, m]
+      scattering 1:  P(n_m) sum_n S0[n, m] (if los) + sum_p vis2 S2(p, m; P(n_p) e_p),  e_p = sum_n S1[n, p]
+    (S the em_wave pair field, P the tangential projection), which equals the sum of
+    path_field over workchunkingv2's rows."""
+    m0, m1, m2, _ = masks
+    kw = dict(self_to_self=True, cull=False, eps=NUMBA_EPSILON)
+    M = _f3(snk).shape[0]
+    out = np.zeros((M, 3), np.complex128)
+    if scattering == 0 or los:
+        out = sink_field(src, srcE, snk, snk_nrm, alpha, beta, mask=m0, **kw)
+    if scattering >= 1:
+        out = _proj(out, _f3(snk_nrm).astype(np.float64))
+        if _f3(scat).shape[0]:
+            e_p = sink_field(src, srcE, scat, scat_nrm, alpha, beta, mask=m1, **kw)
+            u_p = _proj(e_p, _f3(scat_nrm).astype(np.float64))
+            out = out + sink_field(scat, u_p, snk, snk_nrm, alpha, beta, mask=m2, **kw)
+    return out

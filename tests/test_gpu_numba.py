@@ -1,0 +1,140 @@
+"""GPU parity of the numba-engine entry points against the oracle's restatement.
+
+workchunkingv2's path index must equal the oracle's row for row (visibility
+is bit-exact); EMGPUFreqDomain and calculate_scattering(cuda=False) must be
+within 1e-5 (max-normalised) of the oracle's FP64 per-path product."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+
+from helpers import random_scene, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from lyceanem_gb300 import build
+    build.build_native()
+
+
+def _scene(seed=3, n_src=6, n_snk=40, n_tris=80, n_scat=25):
+    src, snk, snk_n, v, f, E = random_scene(seed, n_src=n_src, n_snk=n_snk, n_tris=n_tris)
+    rng = np.random.default_rng(seed + 10)
+    scat = rng.uniform(-1, 1, (n_scat, 3)).astype(np.float32)
+    scat_n = rng.normal(size=(n_scat, 3)).astype(np.float32)
+    scat_n /= np.linalg.norm(scat_n, axis=1, keepdims=True)
+    return src, snk, snk_n, v, f, E, scat, scat_n
+
+
+def _no_device_errors():
+    from lyceanem_gb300 import propagation as P
+    assert P.device_errors() == (0, 0)
+
+
+@pytest.mark.parametrize("max_scatter,los", [(1, True), (2, True), (2, False), (3, True), (3, False)])
+def test_workchunkingv2_matches_oracle(max_scatter, los):
+    from lyceanem_gb300 import raycasting as RC
+    src, snk, snk_n, v, f, E, scat, scat_n = _scene()
+    idx, rays = RC.workchunkingv2(src, snk, scat, (v, f), max_scatter, line_of_sight=los)
+    masks = O.numba_masks(src, snk, scat, O.pack_triangles(v, f))
+    oidx, orays = O.numba_path_index(src.shape[0], snk.shape[0], scat.shape[0], *masks, max_scatter,
+                                     line_of_sight=los)
+    assert idx.dtype == np.int32 and np.array_equal(idx, oidx)
+    assert rays == orays
+    # the triangle_t records of convertTriangles give the same index
+    from lyceanem_gb300.geometry import Mesh
+    recs = RC.convertTriangles(Mesh(v, [("triangle", f)]))
+    idx2, _ = RC.workchunkingv2(src, snk, scat, recs, max_scatter, line_of_sight=los)
+    assert np.array_equal(idx2, idx)
+    _no_device_errors()
+
+
+def _points(src, snk, snk_n, scat, scat_n, E, rng):
+    from lyceanem_gb300.empropagation import scattering_point
+    N, M, Pn = src.shape[0], snk.shape[0], scat.shape[0]
+    pts = np.zeros(N + M + Pn, dtype=scattering_point)
+    pos = np.concatenate([src, snk, scat])
+    nrm = np.concatenate([np.tile([[0, 0, 1.0]], (N, 1)), snk_n, scat_n]).astype(np.float32)
+    w = (rng.normal(size=(N + M + Pn, 3)) + 1j * rng.normal(size=(N + M + Pn, 3))).astype(np.complex64)
+    w[:N] = E
+    for k, c in enumerate("xyz"):
+        pts[f"p{c}"] = pos[:, k]
+        pts[f"n{c}"] = nrm[:, k]
+        pts[f"e{c}"] = w[:, k]
+    pts["Electric"] = True
+    pts["permittivity"] = 8.8541878176e-12
+    pts["permeability"] = 1.25663706212e-6
+    return pts, pos, nrm, w
+
+
+@pytest.mark.parametrize("max_scatter", [1, 2, 3])
+def test_emgpufreqdomain_vs_oracle(max_scatter):
+    from lyceanem_gb300 import raycasting as RC
+    from lyceanem_gb300.empropagation import EMGPUFreqDomain
+    src, snk, snk_n, v, f, E, scat, scat_n = _scene(seed=5)
+    rng = np.random.default_rng(7)
+    pts, pos, nrm, w = _points(src, snk, snk_n, scat, scat_n, E, rng)
+    N, M = src.shape[0], snk.shape[0]
+    idx, _ = RC.workchunkingv2(src, snk, scat, (v, f), max_scatter)
+    beta = 2 * np.pi / 0.05
+    S = EMGPUFreqDomain(N, M, idx, pts, 0.05, 0.02, beta)
+    So = O.path_field(idx, pos, nrm, w, N, M, 0.02, beta)
+    assert S.shape == (N, M, 3) and S.dtype == np.complex128
+    assert rel_err(S, So) < FIELD_TOL
+    # magnetic sources: the launched field is (w x d) / sqrt(mu / eps)
+    pts["Electric"][: N // 2] = False
+    mag = ~pts["Electric"]
+    imp = np.sqrt(np.real(pts["permeability"]) / np.real(pts["permittivity"])).astype(np.float32)
+    S = EMGPUFreqDomain(N, M, idx, pts, 0.05, 0.02, beta)
+    So = O.path_field(idx, pos, nrm, w, N, M, 0.02, beta, magnetic=mag, impedance=imp)
+    assert rel_err(S, So) < FIELD_TOL
+    _no_device_errors()
+
+
+def test_emgpufreqdomain_rejects_bad_rows():
+    from lyceanem_gb300._native import LyemError
+    from lyceanem_gb300.empropagation import EMGPUFreqDomain
+    src, snk, snk_n, v, f, E, scat, scat_n = _scene(seed=6, n_scat=4)
+    pts, _, _, _ = _points(src, snk, snk_n, scat, scat_n, E, np.random.default_rng(1))
+    bad = np.array([[1, 10_000, 0]], np.int32)  # an index past the last point
+    with pytest.raises(LyemError):
+        EMGPUFreqDomain(src.shape[0], snk.shape[0], bad, pts, 0.05, 0.0, 100.0)
+
+
+@pytest.mark.parametrize("scattering,los,elements", [(0, True, False), (1, True, False), (1, False, False),
+                                                     (1, True, True), (2, True, False)])
+def test_calculate_scattering_numba_branch(scattering, los, elements):
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import frequency_domain as FD
+    src, snk, snk_n, v, f, E, scat, scat_n = _scene(seed=8, n_src=5, n_snk=50, n_tris=90, n_scat=20)
+    N, M, Pn = src.shape[0], snk.shape[0], scat.shape[0]
+    solid = Mesh(v, [("triangle", f)])
+    ap = Mesh(src, point_data={"Normals": np.tile([[0, 0, 1.0]], (N, 1)), "Area": np.full(N, 0.5)})
+    sk = Mesh(snk, point_data={"Normals": snk_n})
+    sc = Mesh(scat, point_data={"Normals": scat_n})
+    beta = 2 * np.pi / 0.04
+    axis = np.array([[1.0, 0.0, 0.0]])
+    out = FD.calculate_scattering(ap, sk, solid, axis, scatter_points=sc, wavelength=0.04, scattering=scattering,
+                                  elements=elements, los=los, beta=beta, cuda=False)
+    got = np.stack(out, -1)
+    # excitation of the numba branch: areas with scattering 0, the bare first row otherwise
+    Esrc = np.tile(axis * (0.5 if scattering == 0 else 1.0), (N, 1)).astype(np.complex64)
+    masks = O.numba_masks(src, snk, scat, O.pack_triangles(v, f))
+    pos = np.concatenate([src, snk, scat])
+    nrm = np.concatenate([np.tile([[0, 0, 1]], (N, 1)), snk_n, scat_n]).astype(np.float32)
+    w = np.ones((N + M + Pn, 3), np.complex128)
+    w[:N] = Esrc
+    idx, _ = O.numba_path_index(N, M, Pn, *masks, scattering + 1, line_of_sight=los)
+    net = O.path_field(idx, pos, nrm, w, N, M, 0.0, beta)
+    ref = net if elements else net.sum(0)
+    assert rel_err(got, ref) < FIELD_TOL
+    if scattering <= 1 and not elements:
+        fact = O.numba_sink_field(src, Esrc, snk, snk_n, scat, scat_n, 0.0, beta, masks, scattering, los=los)
+        assert rel_err(got, fact) < FIELD_TOL
+    _no_device_errors()

@@ -134,3 +134,40 @@ def test_onebounce_factorised_equals_reference_composition():
     got, e_p2 = O.onebounce_sink_field(src, E, snk, snk_n, scat, scat_n, 0.0, beta, tris12=tris)
     assert rel_err(e_p2, e_p) < 1e-12
     assert rel_err(got, ref) < 1e-10
+
+
+def _numba_scene(seed=3):
+    from helpers import random_scene
+    src, snk, snk_n, v, f, E = random_scene(seed, n_src=6, n_snk=40, n_tris=80)
+    rng = np.random.default_rng(seed + 10)
+    scat = rng.uniform(-1, 1, (25, 3)).astype(np.float32)
+    scat_n = rng.normal(size=(25, 3)).astype(np.float32)
+    scat_n /= np.linalg.norm(scat_n, axis=1, keepdims=True)
+    return src, snk, snk_n, v, f, E, scat, scat_n
+
+
+def test_numba_path_product_factorises():
+    """The numba engine's per-path sum (freqdomainkernal over workchunkingv2's rows) equals the
+    factored form the GPU composition uses (direct projected at the sinks, bounce driven by the
+    projected scatter excitation), in FP64."""
+    src, snk, snk_n, v, f, E, scat, scat_n = _numba_scene()
+    masks = O.numba_masks(src, snk, scat, O.pack_triangles(v, f))
+    N, M, Pn = src.shape[0], snk.shape[0], scat.shape[0]
+    pos = np.concatenate([src, snk, scat])
+    nrm = np.concatenate([np.tile([[0, 0, 1]], (N, 1)), snk_n, scat_n]).astype(np.float32)
+    w = np.ones((N + M + Pn, 3), np.complex128)
+    w[:N] = E
+    for max_scatter, los in ((1, True), (2, True), (2, False)):
+        idx, rays = O.numba_path_index(N, M, Pn, *masks, max_scatter, line_of_sight=los)
+        net = O.path_field(idx, pos, nrm, w, N, M, 0.0, 60.0)
+        ref = O.numba_sink_field(src, E, snk, snk_n, scat, scat_n, 0.0, 60.0, masks, max_scatter - 1, los=los)
+        assert np.abs(net.sum(0) - ref).max() <= 1e-12 * np.abs(ref).max()
+        assert rays == N * (M + Pn) if max_scatter == 1 else rays >= N * Pn
+    # two bounces: rows of four columns; direct and one-bounce rows also take the last point's
+    # normal in their projection (the index 0 read as Python's -1)
+    idx, _ = O.numba_path_index(N, M, Pn, *masks, 3)
+    assert idx.shape[1] == 4 and np.all(idx[:, 0] >= 1)
+    full = idx[np.all(idx != 0, axis=1)]
+    assert np.all(full[:, 1] != full[:, 2])
+    net = O.path_field(idx, pos, nrm, w, N, M, 0.0, 60.0)
+    assert np.all(np.isfinite(net))
