@@ -328,6 +328,20 @@ LYEM_API int lyem_path_field(const int32_t *d_paths, int64_t n_paths, int32_t n_
                              const float *d_impedance, int64_t n_pts, int64_t n_src, int64_t n_snk, double alpha,
                              double beta, double *d_out, void *stream);
 
+/* Time-domain form of the same rows (timedomainkernal,
+ * lyceanem/electromagnetics/empropagation.py:1346-1560): per row the real
+ * magnitude vector d_amp [n_paths,3] (real parts of the weights, the same
+ * projections, |loss| of the segments), the arrival time d_arrival [n_paths]
+ * in seconds (path length / c plus the imaginary parts of the x weights of the
+ * source and of each later point; for i >= 1 the length adds the distance to
+ * the point of index row[i+1] even when it is 0, read as the last point, as
+ * the reference does) and d_pair [n_paths,2] (source, sink), or (-1, -1) with
+ * device error bit 1 for a row with an index out of range. */
+LYEM_API int lyem_path_time(const int32_t *d_paths, int64_t n_paths, int32_t n_cols, const float *d_pos,
+                            const float *d_nrm, const float *d_w, const uint8_t *d_magnetic, const float *d_impedance,
+                            int64_t n_pts, int64_t n_src, int64_t n_snk, double alpha, double beta, double *d_amp,
+                            double *d_arrival, int32_t *d_pair, void *stream);
+
 /* ------------------------------------------ host mirrors of lyceanem.em */
 
 /* bin_counts_to_numpy (lyceanem/src/terrain_acceleration_build.cuh:296-348):

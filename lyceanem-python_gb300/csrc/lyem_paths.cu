@@ -175,6 +175,100 @@ __global__ void path_field_kernel(const PathParams p) {
     }
 }
 
+// Time-domain form of the same row walk (timedomainkernal,
+// lyceanem/electromagnetics/empropagation.py:1346-1560): real magnitudes
+// (the real parts of the weights, the same projections), |loss| of the
+// segments, and the arrival time = path length / c + the imaginary parts of
+// the x weights of the source and of every later point ("time delays").  The
+// path length adds, for i >= 1, the distance from a_i to the point of index
+// a_{i+1} even when that index is 0 (then the last point), as the reference does.
+__global__ void path_time_kernel(const PathParams p, double* amp, double* arrival, int32_t* pair) {
+    const double kC = 299792458.0;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < p.n_paths;
+         r += (long long)gridDim.x * blockDim.x) {
+        const int32_t* row = p.paths + r * p.cols;
+        bool bad = false;
+        int last = 0;
+        for (int i = 0; i < p.cols; ++i) {
+            const int v = row[i];
+            if (v < 0 || v > p.n_pts) bad = true;
+            if (v != 0) last = v;
+        }
+        const long long src = (long long)row[0] - 1;
+        const long long snk = (long long)last - p.n_src - 1;
+        if (bad || src < 0 || src >= p.n_src || row[1] == 0 || snk < 0 || snk >= p.n_snk) {
+            atomicOr(p.err, 2u);
+            pair[2 * r] = -1;
+            pair[2 * r + 1] = -1;
+            continue;
+        }
+        auto pt = [&](int v) -> long long { return v > 0 ? (long long)v - 1 : p.n_pts - 1; };
+        const long long a0 = pt(row[0]), a1 = pt(row[1]);
+        float f[3];
+        const float* wa = p.w + 6 * a0;
+        double delay = (double)wa[1];
+        if (p.magnetic && p.magnetic[a0]) {
+            const Ray d = make_ray(p.pos[3 * a0], p.pos[3 * a0 + 1], p.pos[3 * a0 + 2], p.pos[3 * a1],
+                                   p.pos[3 * a1 + 1], p.pos[3 * a1 + 2]);
+            const float dd[3] = {d.dx, d.dy, d.dz};
+            const float inv_eta = p.impedance ? 1.0f / p.impedance[a0] : 1.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+                f[k] = (wa[2 * k1] * dd[k2] - wa[2 * k2] * dd[k1]) * inv_eta;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) f[k] = wa[2 * k];
+        }
+        float mag = 1.f;
+        double length = 0.0;
+        for (int i = 0; i + 1 < p.cols; ++i) {
+            const long long ai = pt(row[i]);
+            const long long bi = pt(row[i + 1]);
+            const float* pa = p.pos + 3 * ai;
+            const float* pb = p.pos + 3 * bi;
+            if (i > 0) {
+                C3 g;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    g.re[k] = f[k];
+                    g.im[k] = 0.f;
+                }
+                project(g, p.nrm[3 * ai], p.nrm[3 * ai + 1], p.nrm[3 * ai + 2]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) f[k] = g.re[k];
+            }
+            if (ai != bi) {  // the same point twice (two 0 indices read as the last point) adds nothing
+                const Ray d = make_ray(pa[0], pa[1], pa[2], pb[0], pb[1], pb[2]);
+                if (d.len > 0.f) length += path_length_fp64(pa[0], pa[1], pa[2], pb[0], pb[1], pb[2], d.len);
+            }
+            if (row[i + 1] != 0) {
+                const Ray d = make_ray(pa[0], pa[1], pa[2], pb[0], pb[1], pb[2]);
+                C3 g;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    g.re[k] = f[k];
+                    g.im[k] = 0.f;
+                }
+                project(g, d.dx, d.dy, d.dz);
+                const float* wb = p.w + 6 * bi;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) f[k] = g.re[k] * wb[2 * k];
+                delay += (double)wb[1];
+                float sr, si;
+                seg_loss(pa, pb, p.nrm + 3 * bi, p.alpha, p.beta_f, p.beta_d, sr, si);
+                mag *= sqrtf(sr * sr + si * si);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) amp[3 * r + k] = (double)(f[k] * mag);
+        arrival[r] = length / kC + delay;
+        pair[2 * r] = (int32_t)src;
+        pair[2 * r + 1] = (int32_t)snk;
+    }
+}
+
 unsigned grid_for(long long n) {
     long long b = (n + 255) / 256;
     return (unsigned)(b < 1 ? 1 : (b > 152LL * 16 ? 152LL * 16 : b));
@@ -228,6 +322,44 @@ LYEM_API int lyem_path_field(const int32_t* d_paths, int64_t n_paths, int32_t n_
     p.out = d_out;
     p.err = device_error_word();
     path_field_kernel<<<grid_for(n_paths), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p);
+    note_launches(1);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        record_cuda_error(e);
+        return LYEM_ERR_CUDA;
+    }
+    return LYEM_OK;
+}
+
+LYEM_API int lyem_path_time(const int32_t* d_paths, int64_t n_paths, int32_t n_cols, const float* d_pos,
+                            const float* d_nrm, const float* d_w, const uint8_t* d_magnetic, const float* d_impedance,
+                            int64_t n_pts, int64_t n_src, int64_t n_snk, double alpha, double beta, double* d_amp,
+                            double* d_arrival, int32_t* d_pair, void* stream) {
+    if (n_paths < 0 || n_cols < 2 || n_cols > 16 || n_pts < 0 || n_src < 0 || n_snk < 0) return LYEM_ERR_INVALID;
+    if (n_paths == 0) return LYEM_OK;
+    if (!d_paths || !d_pos || !d_nrm || !d_w || !d_amp || !d_arrival || !d_pair || n_pts == 0)
+        return LYEM_ERR_INVALID;
+    if (n_pts >= (1LL << 31) || n_src + n_snk > n_pts) return LYEM_ERR_INVALID;
+    if (((uintptr_t)d_amp & 7u) || ((uintptr_t)d_arrival & 7u) || ((uintptr_t)d_w & 7u)) return LYEM_ERR_INVALID;
+    PathParams p;
+    p.paths = d_paths;
+    p.n_paths = n_paths;
+    p.cols = n_cols;
+    p.pos = d_pos;
+    p.nrm = d_nrm;
+    p.w = d_w;
+    p.magnetic = d_magnetic;
+    p.impedance = d_impedance;
+    p.n_pts = n_pts;
+    p.n_src = n_src;
+    p.n_snk = n_snk;
+    p.alpha = (float)alpha;
+    p.beta_f = (float)beta;
+    p.beta_d = beta;
+    p.out = nullptr;
+    p.err = device_error_word();
+    path_time_kernel<<<grid_for(n_paths), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(p, d_amp, d_arrival,
+                                                                                           d_pair);
     note_launches(1);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

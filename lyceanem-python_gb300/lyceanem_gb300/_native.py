@@ -104,6 +104,8 @@ SIGNATURES = {
     "lyem_tangential_project": ([_vp, _vp, _i64, _vp], ctypes.c_int),
     "lyem_path_field": ([_vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _f64, _f64, _vp, _vp],
                         ctypes.c_int),
+    "lyem_path_time": ([_vp, _i64, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _f64, _f64, _vp, _vp, _vp, _vp],
+                       ctypes.c_int),
     "lyem_em_bin_counts": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp], ctypes.c_int),
     "lyem_em_bin_triangles": ([_vp, _i64, _vp, _i64, _i32, _i32, _f32, _f32, _f32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_em_calculate_scattering_brute_force": (

@@ -72,3 +72,76 @@ def tangential_project(vec, normals):
     v = torch.view_as_real(vec)
     check(lib.lyem_tangential_project(_vp(v), _vp(nrm), vec.shape[0], P._stream()), "tangential_project")
     return vec
+
+
+def path_times(full_index, pos, nrm, weights, n_src, n_snk, alpha, beta, magnetic=None, impedance=None):
+    """Per path row (CUDA tensors): real magnitude vector float64 [R,3], arrival time float64 [R] (s)
+    and (source, sink) int32 [R,2] -- the per-row part of timedomainkernal."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    idx = torch.as_tensor(np.ascontiguousarray(np.asarray(full_index), dtype=np.int32), device=dev)
+    pos = P._points(pos)
+    nrm = P._points(nrm)
+    w = torch.view_as_real(P._cvec(weights, pos.shape[0])).reshape(-1, 6).contiguous()
+    mag = imp = None
+    if magnetic is not None and np.any(np.asarray(magnetic)):
+        mag = torch.as_tensor(np.asarray(magnetic, dtype=np.uint8), device=dev)
+        imp = torch.as_tensor(np.asarray(impedance, dtype=np.float32), device=dev)
+    R, K = (idx.shape[0], idx.shape[1]) if idx.dim() == 2 else (0, 2)
+    amp = torch.zeros((R, 3), dtype=torch.float64, device=dev)
+    arrival = torch.zeros(R, dtype=torch.float64, device=dev)
+    pair = torch.zeros((R, 2), dtype=torch.int32, device=dev)
+    check(lib.lyem_path_time(_vp(idx), R, K, _vp(pos), _vp(nrm), _vp(w), _vp(mag), _vp(imp), pos.shape[0], n_src,
+                             n_snk, float(alpha), float(beta), _vp(amp), _vp(arrival), _vp(pair), P._stream()),
+          "path_time")
+    st, flags = P.device_errors()
+    if st != 0 or flags != 0:
+        raise LyemError(st or 1, f"path_time: device error word {flags:#x} (an index out of range)")
+    return amp, arrival, pair
+
+
+def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples):
+    """float64 [n_src, n_snk, num_samples, 3] (CUDA): each row's excitation, scaled by its magnitudes,
+    starting at floor((arrival - wake) / (1 / sampling_freq)) samples and cut at num_samples, with
+    wake = the earliest arrival; returned with wake.  Built as an amplitude histogram of arrival
+    samples per (source, sink) convolved with the excitation (FFT)."""
+    dev = amp.device
+    S = int(num_samples)
+    exc = torch.as_tensor(np.asarray(excitation, np.float64), device=dev).reshape(-1)
+    if arrival.numel() == 0:
+        return torch.zeros((n_src, n_snk, S, 3), dtype=torch.float64, device=dev), 1.0
+    wake = float(arrival.min().item())
+    step = torch.tensor(1.0 / sampling_freq, dtype=torch.float64, device=dev)
+    t0 = torch.div(arrival - wake, step, rounding_mode="floor").to(torch.int64)
+    keep = t0 < S
+    h = torch.zeros((n_src * n_snk * S, 3), dtype=torch.float64, device=dev)
+    flat = (pair[:, 0].long() * n_snk + pair[:, 1].long()) * S + t0
+    h.index_add_(0, flat[keep], amp[keep])
+    h = h.reshape(n_src * n_snk, S, 3).permute(0, 2, 1)  # [series, 3, S]
+    n = 1
+    while n < S + exc.numel():
+        n *= 2
+    y = torch.fft.irfft(torch.fft.rfft(h, n=n) * torch.fft.rfft(exc, n=n), n=n)[..., :S]
+    return y.permute(0, 2, 1).reshape(n_src, n_snk, S, 3).contiguous(), wake
+
+
+def TimeDomainv3(source_num, sink_num, point_informationv2, full_index, scattering_coefficient, wavelength,
+                 excitation_signal, sampling_freq, num_samples, alpha, beta):
+    """(time_map float64 [source_num, sink_num, num_samples, 3], wake_times [1]) of
+    lyceanem/electromagnetics/empropagation.py:2910-3170 (the single-chunk form: one wake time,
+    the earliest arrival over all rows; the reference takes it with an atomic minimum that is only
+    synchronised within a thread block, so its value there can depend on block scheduling)."""
+    del scattering_coefficient, wavelength  # unused by the reference's kernel
+    pts = np.asarray(point_informationv2)
+    pos = np.stack([pts["px"], pts["py"], pts["pz"]], 1).astype(np.float32)
+    nrm = np.stack([pts["nx"], pts["ny"], pts["nz"]], 1).astype(np.float32)
+    w = np.stack([pts["ex"], pts["ey"], pts["ez"]], 1).astype(np.complex64)
+    magnetic = impedance = None
+    if "Electric" in pts.dtype.names and not np.all(pts["Electric"]):
+        magnetic = ~pts["Electric"].astype(bool)
+        impedance = np.sqrt(np.real(pts["permeability"]).astype(np.float64)
+                            / np.real(pts["permittivity"]).astype(np.float64)).astype(np.float32)
+    amp, arrival, pair = path_times(full_index, pos, nrm, w, int(source_num), int(sink_num), alpha, beta, magnetic,
+                                    impedance)
+    tm, wake = time_map(amp, arrival, pair, int(source_num), int(sink_num), excitation_signal, sampling_freq,
+                        num_samples)
+    return tm.cpu().numpy(), np.array([wake], dtype=np.float64)

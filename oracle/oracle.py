@@ -364,3 +364,57 @@ def numba_sink_field(src, srcE, snk, snk_nrm, scat, scat_nrm, alpha, beta, masks
             u_p = _proj(e_p, _f3(scat_nrm).astype(np.float64))
             out = out + sink_field(scat, u_p, snk, snk_nrm, alpha, beta, mask=m2, **kw)
     return out
+
+
+def path_times(full_index, pos, nrm, w, n_src, n_snk, alpha, beta, magnetic=None, impedance=None):
+    """FP64 per-row part of timedomainkernal (lyceanem/electromagnetics/empropagation.py:1346-1560):
+    real magnitude vector (R,3), arrival time (R,) and (source, sink) (R,2).  The path length adds,
+    for i >= 1, the distance to the point of index row[i+1] even when it is 0 (the last point)."""
+    idx = np.asarray(full_index, dtype=np.int64)
+    pos = np.asarray(pos, np.float32).astype(np.float64)
+    nrm = np.asarray(nrm, np.float32).astype(np.float64)
+    w = np.asarray(w).astype(np.complex128)
+    npt = pos.shape[0]
+    pt = np.where(idx > 0, idx - 1, npt - 1)
+    R, K = idx.shape
+    a0, a1 = pt[:, 0], pt[:, 1]
+    f = w[a0].real.copy()
+    delay = w[a0, 0].imag.copy()
+    if magnetic is not None and np.any(np.asarray(magnetic)[a0]):
+        sel = np.asarray(magnetic, bool)[a0]
+        d = pos[a1] - pos[a0]
+        d /= np.linalg.norm(d, axis=-1, keepdims=True)
+        f[sel] = np.cross(w[a0].real[sel], d[sel]) / np.asarray(impedance, np.float64)[a0][sel][:, None]
+    mag = np.ones(R)
+    length = np.zeros(R)
+    for i in range(K - 1):
+        ai, bi = pt[:, i], pt[:, i + 1]
+        if i > 0:
+            f = _proj(f, nrm[ai])
+        length += np.linalg.norm(pos[bi] - pos[ai], axis=-1)
+        has = idx[:, i + 1] != 0
+        if np.any(has):
+            L, dn = _seg_loss(pos[ai[has]], pos[bi[has]], nrm[bi[has]], alpha, beta)
+            f[has] = _proj(f[has], dn) * w[bi[has]].real
+            delay[has] += w[bi[has], 0].imag
+            mag[has] *= np.abs(L)
+    last = np.zeros(R, np.int64)
+    for i in range(K):
+        last = np.where(idx[:, i] != 0, idx[:, i], last)
+    pair = np.stack([idx[:, 0] - 1, last - n_src - 1], 1)
+    return f * mag[:, None], length / 299792458.0 + delay, pair
+
+
+def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples):
+    """Each row's excitation times its magnitudes, placed at floor((arrival - wake) / (1 / fs))
+    and cut at num_samples (the accumulation of timedomainkernal); returns (map, wake)."""
+    S = int(num_samples)
+    exc = np.asarray(excitation, np.float64).ravel()
+    out = np.zeros((n_src, n_snk, S, 3))
+    wake = float(np.min(arrival))
+    t0 = np.floor_divide(np.asarray(arrival) - wake, 1.0 / sampling_freq).astype(np.int64)
+    for r in range(len(t0)):
+        k = min(exc.size, S - t0[r])
+        if k > 0:
+            out[pair[r, 0], pair[r, 1], t0[r]:t0[r] + k] += exc[:k, None] * amp[r][None]
+    return out, wake
