@@ -148,6 +148,60 @@ def read_ply(source):
     return Mesh(points=pts, cells=[("triangle", faces)])
 
 
+def read_stl(source):
+    """STL file (binary or ASCII, path or bytes) -> Mesh with unique points, one triangle cell block
+    and the facet normals as cell_data["Normals"] (the scenes meshio reads for the reference)."""
+    if isinstance(source, (bytes, bytearray)):
+        raw = bytes(source)
+    else:
+        with open(source, "rb") as fh:
+            raw = fh.read()
+    binary = len(raw) >= 84 and len(raw) == 84 + 50 * int(np.frombuffer(raw[80:84], "<u4")[0])
+    if binary:
+        n = int(np.frombuffer(raw[80:84], "<u4")[0])
+        rec = np.frombuffer(raw[84:84 + 50 * n], dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)),
+                                                                  ("attr", "<u2")]))
+        normals = rec["n"].astype(np.float32)
+        tri = rec["v"].astype(np.float32)
+    else:
+        words = raw.decode("ascii", errors="replace").split()
+        normals, verts = [], []
+        i = 0
+        while i < len(words):
+            w = words[i].lower()
+            if w == "normal":
+                normals.append([float(x) for x in words[i + 1:i + 4]])
+                i += 4
+            elif w == "vertex":
+                verts.append([float(x) for x in words[i + 1:i + 4]])
+                i += 4
+            else:
+                i += 1
+        tri = np.asarray(verts, np.float32).reshape(-1, 3, 3)
+        normals = np.asarray(normals, np.float32).reshape(-1, 3)
+    pts, inv = np.unique(tri.reshape(-1, 3), axis=0, return_inverse=True)
+    faces = inv.reshape(-1, 3).astype(np.int32)
+    return Mesh(pts.astype(np.float32), [("triangle", faces)], cell_data={"Normals": [normals]})
+
+
+def mesh_conversion(conversion_object):
+    """Triangle records (triangle_t layout) of a mesh, a list of meshes, or a structures-like object
+    (lyceanem/geometry/geometryfunctions.py:473-510); anything else gives no triangles."""
+    from .raycasting import convertTriangles, triangle_t
+    if conversion_object is None:
+        return np.empty(0, dtype=triangle_t)
+    if hasattr(conversion_object, "triangles_base_raycaster"):
+        return np.asarray(conversion_object.triangles_base_raycaster())
+    if hasattr(conversion_object, "export_all_structures"):
+        return mesh_conversion(list(conversion_object.export_all_structures()))
+    if isinstance(conversion_object, (list, tuple)):
+        parts = [mesh_conversion(item) for item in conversion_object]
+        return np.concatenate(parts) if parts else np.empty(0, dtype=triangle_t)
+    if hasattr(conversion_object, "points") and hasattr(conversion_object, "cells"):
+        return convertTriangles(conversion_object)
+    return np.empty(0, dtype=triangle_t)
+
+
 def face_normals(vertices, faces):
     v = np.asarray(vertices, dtype=np.float64)
     f = np.asarray(faces)

@@ -13,6 +13,9 @@ reference (lyceanem/models/acceleration_structures.py:72-115).
 sink_field(...) returns the source-summed complex64 [M, 3] field without
 forming the network.
 """
+import collections
+import hashlib
+
 import numpy as np
 import torch
 
@@ -118,6 +121,35 @@ class Tile_acceleration_structure:
 
     def sink_field(self, source_mesh, sink_mesh, alpha, beta, wavelength=None, self_to_self=False):
         return self.device.sink_field(source_mesh, sink_mesh, alpha, beta, self_to_self)
+
+
+# Scene cache: the last few tile structures, keyed by a fingerprint of the geometry and the grid
+# cell, so that repeated model calls on the same solid reuse its device triangles and grid.
+_CACHE = collections.OrderedDict()
+CACHE_SIZE = 4
+cache_stats = {"hits": 0, "misses": 0}
+
+
+def cached_structure(verts, faces, grid_cell=None):
+    """Tile_acceleration_structure of (verts, faces) from the scene cache, built on a miss."""
+    v = np.ascontiguousarray(verts, dtype=np.float32)
+    f = np.ascontiguousarray(faces, dtype=np.int32)
+    h = hashlib.sha1()
+    h.update(v.tobytes())
+    h.update(f.tobytes())
+    key = (h.hexdigest(), v.shape, f.shape, None if grid_cell is None else float(grid_cell),
+           torch.cuda.current_device())
+    if key in _CACHE:
+        cache_stats["hits"] += 1
+        _CACHE.move_to_end(key)
+        return _CACHE[key]
+    cache_stats["misses"] += 1
+    from ..geometry import Mesh
+    acc = Tile_acceleration_structure(Mesh(v, [("triangle", f)]), 1, grid_cell=grid_cell)
+    _CACHE[key] = acc
+    while len(_CACHE) > CACHE_SIZE:
+        _CACHE.popitem(last=False)
+    return acc
 
 
 class Brute_Force_acceleration_structure:

@@ -14,16 +14,17 @@ import numpy as np
 import torch
 
 from .. import propagation as P
-from ..geometry import Mesh, calculate_conformal_vectors, spherical_field, triangles_of
+from ..geometry import calculate_conformal_vectors, spherical_field, triangles_of
 from . import acceleration_structures
 
 
 def _as_structure(antenna_solid, acceleration_structure, grid_cell=None):
+    """The caller's structure, or the device scene of antenna_solid from the scene cache
+    (packed triangles and grid stay on the device across calls with the same geometry)."""
     if acceleration_structure is not None:
         return acceleration_structure
     verts, faces = triangles_of(antenna_solid)
-    mesh = Mesh(verts, [("triangle", faces)])
-    return acceleration_structures.Tile_acceleration_structure(mesh, 1, grid_cell=grid_cell)
+    return acceleration_structures.cached_structure(verts, faces, grid_cell)
 
 
 def _excitation(desired_E_axis, aperture_coords, project_vectors, antenna_axes):

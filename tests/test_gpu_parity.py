@@ -350,3 +350,26 @@ def test_masks_bit_exact_to_reference_device_code(case):
         got = r.pairs.cpu().numpy().reshape(-1, 3)[g["sample"]]
         ref_f = d[f"{case}_fma_field"].astype(np.float32).view(np.complex64).reshape(-1, 3)
         assert np.abs(got - ref_f).max() / np.abs(ref_f).max() < 1e-3
+
+
+def test_scene_cache_reuses_device_grid():
+    """Repeated model calls on the same solid reuse its device triangles and grid; the results are
+    identical and a different solid builds a new scene."""
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import acceleration_structures as A
+    from lyceanem_gb300.models import frequency_domain as FD
+    src, snk, snk_n, v, f, E = random_scene(31, n_src=4, n_snk=50, n_tris=90)
+    ap = Mesh(src, point_data={"Normals": np.tile([[0, 0, 1.0]], (4, 1)), "Area": np.ones(4)})
+    sk = Mesh(snk, point_data={"Normals": snk_n})
+    axis = np.array([0.0, 1.0, 0.0])
+    h0, m0 = A.cache_stats["hits"], A.cache_stats["misses"]
+    first = FD.calculate_scattering(ap, sk, Mesh(v, [("triangle", f)]), axis, beta=150.0)
+    again = FD.calculate_scattering(ap, sk, Mesh(v.copy(), [("triangle", f.copy())]), axis, beta=150.0)
+    assert A.cache_stats["misses"] == m0 + 1 and A.cache_stats["hits"] == h0 + 1
+    for x, y in zip(first, again):
+        assert np.array_equal(x, y)
+    v2 = v.copy()
+    v2[0, 0] += 0.01
+    FD.calculate_scattering(ap, sk, Mesh(v2, [("triangle", f)]), axis, beta=150.0)
+    assert A.cache_stats["misses"] == m0 + 2
+    _no_device_errors()

@@ -70,3 +70,60 @@ def test_sweep_and_batched_recipes_small():
     assert len(sc) == 3 and snk.shape == (100, 3) and freqs.shape == (4,)
     for s in sc:
         assert 900 <= s.faces.shape[0] <= 2100
+
+
+def _stl_bytes_binary(tri, normals):
+    import struct
+    out = bytearray(b"\0" * 80) + struct.pack("<I", tri.shape[0])
+    for t, n in zip(tri, normals):
+        out += struct.pack("<12fH", *n, *t.ravel(), 0)
+    return bytes(out)
+
+
+def _stl_bytes_ascii(tri, normals):
+    lines = ["solid test"]
+    for t, n in zip(tri, normals):
+        lines.append(f"facet normal {n[0]:.9g} {n[1]:.9g} {n[2]:.9g}")
+        lines.append("outer loop")
+        lines += [f"vertex {v[0]:.9g} {v[1]:.9g} {v[2]:.9g}" for v in t]
+        lines += ["endloop", "endfacet"]
+    lines.append("endsolid test")
+    return "\n".join(lines).encode()
+
+
+def test_read_stl_binary_and_ascii():
+    """STL scenes (the format of the reference's test scenes) read to the same triangles either way."""
+    from lyceanem_gb300.geometry import read_stl, triangles_of
+    rng = np.random.default_rng(0)
+    # a closed cube (shared vertices) plus a few loose triangles
+    c = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], np.float32)
+    f = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4], [1, 2, 6], [1, 6, 5],
+                  [2, 3, 7], [2, 7, 6], [3, 0, 4], [3, 4, 7]])
+    tri = np.concatenate([c[f], rng.uniform(-1, 1, (5, 3, 3)).astype(np.float32)])
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]).astype(np.float32)
+    for raw in (_stl_bytes_binary(tri, nrm), _stl_bytes_ascii(tri, nrm)):
+        m = read_stl(raw)
+        v, fc = triangles_of(m)
+        assert fc.shape == (tri.shape[0], 3)
+        assert np.allclose(v[fc], tri, atol=1e-6)
+        assert np.allclose(m.cell_data["Normals"][0], nrm, atol=1e-5)
+        assert v.shape[0] == 8 + 15  # cube vertices shared, loose triangles' vertices distinct
+
+
+def test_mesh_conversion_records():
+    """mesh_conversion of a mesh, a list and a structures-like object (geometryfunctions.py:473-510)."""
+    from lyceanem_gb300.geometry import Mesh, mesh_conversion
+    rng = np.random.default_rng(1)
+    a = Mesh(rng.normal(size=(6, 3)), [("triangle", [[0, 1, 2], [3, 4, 5]])])
+    b = Mesh(rng.normal(size=(3, 3)), [("triangle", [[0, 1, 2]])])
+    ra, rb = mesh_conversion(a), mesh_conversion(b)
+    assert ra.shape == (2,) and np.isclose(ra["v1y"][1], np.float32(a.points[4, 1]))
+    both = mesh_conversion([a, b])
+    assert both.shape == (3,) and np.array_equal(both[2:], rb)
+
+    class Structures:
+        def triangles_base_raycaster(self):
+            return mesh_conversion([a, b])
+
+    assert np.array_equal(mesh_conversion(Structures()), both)
+    assert mesh_conversion(object()).shape == (0,)
