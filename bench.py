@@ -133,6 +133,23 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ ours
+def max_over_ranks(value, device):
+    """The largest of `value` over the ranks of the process group (the slowest replica sets the
+    whole job's time); `value` itself without a group or with one rank."""
+    import torch
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, world, steps, total_ms):
+    """Units per second of the whole job: every rank processes units_per_step each step (weak scaling)."""
+    return units_per_step * world * steps / (total_ms / 1e3)
+
+
 def run_ours(args, rank, world):
     import numpy as np
     import torch
@@ -206,14 +223,10 @@ def run_ours(args, rank, world):
         torch.distributed.barrier()
     launches = P.kernel_launches() - launches0
     clk = clocks.stop()
-    total_ms = sum(a.elapsed_time(b) for a, b in step_ms)
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in step_ms), dev)
     K = args.steps
     ms_per_step = total_ms / K
-    value = paths * world * K / (total_ms / 1e3)  # paths per second over all ranks
+    value = whole_job_rate(paths, world, K, total_ms)
     st, flags = P.device_errors()
     if st != 0 or flags != 0:
         raise RuntimeError(f"device error word {flags:#x}")
