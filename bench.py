@@ -59,6 +59,8 @@ def parse():
                     help="scenes of the batched measurement (the first S of the 64-scene recipe; profiling cases)")
     ap.add_argument("--batched-config", default="",
                     help="fg,chunk,blocks_per_sm for the batched launch instead of the autotuner (profiling cases)")
+    ap.add_argument("--batched-cell-scale", type=float, default=0.0,
+                    help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
     return ap.parse_args()
 
@@ -375,15 +377,17 @@ def run_sweep(args, n_check=256, reps=5):
 
 
 # ------------------------------------------------------------------ batched
-BATCH_TUNE_CANDIDATES = [(2, 64, 8), (1, 64, 8), (4, 64, 8), (4, 64, 4)]
+BATCH_TUNE_CANDIDATES = [(2, 64, 8), (1, 64, 8), (4, 64, 8)]
+# grid cell edge per scene = k * (box volume / triangles)^(1/3); the autotuner picks k
+BATCH_TUNE_CELL_SCALES = [0.7, 1.0, 1.4]
 
 
 def run_batched(args, reps=2):
     """Batched uneven workload: 64 scenes (square half-wave arrays of 16-16,384 elements and 1e3-5e5
     triangles, both log-uniform, ground + clutter recipe scaled to the count, scatter points on 10% of the
     triangles up to 10,000), 10,000 Fibonacci sinks at 50 m, 64 frequencies 24-30 GHz, direct + one bounce.
-    One persistent launch per step, replayed from a captured CUDA graph; configuration picked by the
-    autotuner on a cost-stratified quarter of the scenes.  Checked against the per-scene pair-stage path
+    One persistent launch per step, replayed from a captured CUDA graph; configuration and grid cell
+    scale picked by the autotuner on a cost-stratified quarter of the scenes.  Checked against the per-scene pair-stage path
     (three scenes, first/middle/last frequency) and against the FP64 oracle on the smallest scene."""
     import numpy as np
     import torch
@@ -394,17 +398,21 @@ def run_batched(args, reps=2):
     from oracle import oracle as O
     scenes, snk, snk_n, freqs = SC.batched_scenes(n_scenes=args.batched_scenes)
     t0 = time.time()
-    bs = B.BatchedScattering(scenes, snk, snk_n, freqs)
+    fixed = args.batched_config and args.batched_cell_scale > 0
+    bs = B.BatchedScattering(scenes, snk, snk_n, freqs, cell_scale=args.batched_cell_scale if fixed else 1.0)
     torch.cuda.synchronize()
     setup_s = time.time() - t0
     t0 = time.time()
-    if args.batched_config:
+    if fixed:
         bs.configure(tuple(int(v) for v in args.batched_config.split(",")))
         tune = {}
     else:
         proxy = B.BatchedScattering([scenes[i] for i in B.stratified_subset(scenes, snk.shape[0])], snk, snk_n,
-                                    freqs)
-        tune = bs.autotune(candidates=BATCH_TUNE_CANDIDATES, proxy=proxy, use_cache=False)
+                                    freqs, cell_scale=1.0)
+        cands = [tuple(int(v) for v in args.batched_config.split(","))] if args.batched_config else \
+            BATCH_TUNE_CANDIDATES
+        scales = [args.batched_cell_scale] if args.batched_cell_scale > 0 else BATCH_TUNE_CELL_SCALES
+        tune = bs.autotune(candidates=cands, proxy=proxy, use_cache=False, cell_scales=scales)
         del proxy
         torch.cuda.empty_cache()
     tune_s = time.time() - t0
@@ -430,7 +438,9 @@ def run_batched(args, reps=2):
            "triangles_total": int(sum(d.n_tris for d in bs.data)),
            "scatter_total": int(sum(d.scat.shape[0] for d in bs.data)),
            "config": {"freq_group": bs.config[0], "src_chunk": bs.config[1], "blocks_per_sm": bs.config[2],
-                      "blocks": bs.blocks, "grid_cell_m": 0.5},
+                      "blocks": bs.blocks, "cell_scale": bs.cell_scale,
+                      "grid_cell_m": {"min": min(bs.grid_cells()), "median": statistics.median(bs.grid_cells()),
+                                      "max": max(bs.grid_cells())}},
            "autotune_ms": {str(list(k)): v for k, v in tune.items()}, "autotune_s": tune_s, "setup_s": setup_s,
            "items": bs.items(), "ms_per_launch": ms, "ms_runs": times,
            "paths_per_launch": paths, "paths_per_s": paths / (ms / 1e3),

@@ -15,7 +15,9 @@ the whole batch; `capture()` records it in a CUDA graph that `run()` replays.
 tile, 256 / ceil(F / group)), the sources per visibility item (the rays of a
 block's tile) and the resident blocks per SM by timing the candidates on the
 batch itself, and remembers the choice in a JSON cache keyed by the device and
-the batch's sizes.
+the batch's sizes.  Given cell_scales it also picks the grid's cell edge per
+scene, k * (box volume / triangles)^(1/3) with one k for the batch: visibility,
+and so the field, is the same for every grid; only the traversal work changes.
 """
 import ctypes
 import hashlib
@@ -70,6 +72,14 @@ def is_uniform(betas):
     return bool(dev <= 1e-12 * max(np.abs(b).max(), 1.0))
 
 
+def density_cell(bounds, n_tris, scale):
+    """Grid cell edge for a scene: scale * (volume of the triangles' box / triangle count)^(1/3),
+    i.e. about scale^-3 triangles per cell, clipped to [0.05, 10] m."""
+    lo, hi = np.asarray(bounds[:3], np.float64), np.asarray(bounds[3:], np.float64)
+    vol = float(np.prod(np.maximum(hi - lo, 1e-3)))
+    return float(np.clip(scale * (vol / max(int(n_tris), 1)) ** (1.0 / 3.0), 0.05, 10.0))
+
+
 class _SceneData:
     """Device-resident data of one scene: sources, mesh grid, scatter points in Morton order."""
 
@@ -80,6 +90,8 @@ class _SceneData:
         self.Ef = torch.view_as_real(self.E).reshape(n, 6).contiguous()
         tris = P.pack_triangles(verts, faces)
         self.n_tris = tris.shape[0]
+        if callable(grid_cell):
+            grid_cell = grid_cell(P.triangle_bounds(tris) if self.n_tris else [0, 0, 0, 1, 1, 1], self.n_tris)
         self.grid = P.UniformGrid(tris, cell=grid_cell)
         if scat is not None and len(scat):
             s = P._points(scat)
@@ -115,6 +127,9 @@ class _SceneData:
 class BatchedScattering:
     """Direct + one-bounce sink fields of many scenes at many frequencies.
 
+    grid_cell: the grid's cell edge in metres, one value or one per scene (None: about one cell per
+      triangle).  cell_scale k (instead): per-scene cells from the scene's triangle density,
+      k * (box volume / triangles)^(1/3) (density_cell); autotune() can choose k.
     scenes: sequence of objects with attributes (or dict keys) src [N,3],
       verts [V,3], faces [T,3], optionally E [N,3] complex (default +x),
       scat [P,3] and scat_n [P,3] (scatter points and normals; P may be 0).
@@ -123,7 +138,7 @@ class BatchedScattering:
     Output of run(): complex64 [n_scenes, n_freq, M, 3] on the device."""
 
     def __init__(self, scenes, sinks, sink_normals, frequencies=None, *, betas=None, alpha=0.0, grid_cell=0.5,
-                 self_to_self=False, cull=True, eps=P.EPSILON, config=None):
+                 self_to_self=False, cull=True, eps=P.EPSILON, config=None, cell_scale=None):
         if betas is None:
             betas = betas_of(frequencies)
         self.betas = np.ascontiguousarray(np.asarray(betas, np.float64).ravel())
@@ -135,8 +150,14 @@ class BatchedScattering:
                 return s.get(k)
             return getattr(s, k, None)
 
+        scenes = list(scenes)
+        if cell_scale is not None:
+            grid_cell = lambda bounds, n_tris: density_cell(bounds, n_tris, cell_scale)  # noqa: E731
+        cells = list(grid_cell) if isinstance(grid_cell, (list, tuple, np.ndarray)) else [grid_cell] * len(scenes)
+        if len(cells) != len(scenes):
+            raise ValueError("grid_cell: one value, or one per scene")
         self.data = [_SceneData(get(s, "src"), get(s, "E"), get(s, "verts"), get(s, "faces"), get(s, "scat"),
-                                get(s, "scat_n"), grid_cell) for s in scenes]
+                                get(s, "scat_n"), c) for s, c in zip(scenes, cells)]
         snk = P._points(sinks)
         snk_n = P._points(sink_normals)
         self.snk_id = P.spatial_order(snk)
@@ -152,7 +173,21 @@ class BatchedScattering:
         self.graph = None
         self.ws = None
         self.blocks = 0
+        self.cell_scale = None if cell_scale is None else float(cell_scale)
         self.configure(config if config is not None else self._default())
+
+    def set_cell_scale(self, scale):
+        """Rebuild every scene's grid with the density rule at `scale` (density_cell) and rewrite the
+        work list; results do not depend on the grid, only the traversal work does."""
+        for d in self.data:
+            g = d.grid
+            d.grid = P.UniformGrid(g.tris, cell=density_cell(g.bounds, d.n_tris, scale))
+        self.cell_scale = float(scale)
+        self._structs = (BatchScene * self.n_scenes)(*[d.struct() for d in self.data])
+        self.configure(self.config)
+
+    def grid_cells(self):
+        return [d.grid.cell for d in self.data]
 
     # ------------------------------------------------------------ configuration
 
@@ -246,17 +281,19 @@ class BatchedScattering:
 
     # ------------------------------------------------------------ autotuner
 
-    def signature(self):
+    def signature(self, cell_scales=None):
         sizes = [(d.src.shape[0], d.scat.shape[0], d.n_tris) for d in self.data]
-        h = hashlib.sha1(json.dumps([sizes, self.n_snk, self.n_freq, self.uniform, self.cull]).encode()).hexdigest()
-        return f"{torch.cuda.get_device_name(self.device)}|{h}"
+        mode = list(cell_scales) if cell_scales else [round(c, 6) for c in self.grid_cells()]
+        h = hashlib.sha1(json.dumps([sizes, self.n_snk, self.n_freq, self.uniform, self.cull, mode]).encode())
+        return f"{torch.cuda.get_device_name(self.device)}|{h.hexdigest()}"
 
-    def autotune(self, candidates=None, reps=1, use_cache=True, log=None, proxy=None):
+    def autotune(self, candidates=None, reps=1, use_cache=True, log=None, proxy=None, cell_scales=None):
         """Times each candidate configuration (one warm launch, then `reps` timed ones) on
         this batch, or on `proxy` (a smaller BatchedScattering with the same frequencies,
         e.g. a cost-stratified subset of the scenes), keeps the fastest for this batch and
-        returns {config: ms}."""
-        key = self.signature()
+        returns {config: ms}.  With cell_scales, each scale of the density rule for the grid
+        cells (set_cell_scale) is tried with every candidate, and the keys are config + (scale,)."""
+        key = self.signature(cell_scales)
         path = _cache_path()
         cache = {}
         if use_cache and os.path.exists(path):
@@ -266,34 +303,47 @@ class BatchedScattering:
             except (OSError, ValueError):
                 cache = {}
         if use_cache and key in cache:
-            self.configure(tuple(cache[key]["config"]))
-            return {tuple(cache[key]["config"]): cache[key]["ms"]}
+            best = tuple(cache[key]["config"])
+            if cell_scales and len(best) == 4:
+                self.config = best[:3]
+                self.set_cell_scale(best[3])
+            else:
+                self.configure(best[:3])
+            return {best: cache[key]["ms"]}
         cands = candidates or CANDIDATES
         if not self.uniform:
             cands = sorted({(1, c[1], c[2]) for c in cands})
         target = proxy if proxy is not None else self
         results = {}
-        for c in cands:
-            try:
-                target.configure(c)
-            except (ValueError, LyemError):
-                continue
-            target.launch()
-            torch.cuda.synchronize()
-            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            t0.record()
-            for _ in range(reps):
+        for scale in (cell_scales or [None]):
+            if scale is not None:
+                target.set_cell_scale(scale)
+            for c in cands:
+                try:
+                    target.configure(c)
+                except (ValueError, LyemError):
+                    continue
                 target.launch()
-            t1.record()
-            torch.cuda.synchronize()
-            results[c] = t0.elapsed_time(t1) / reps
-            if log:
-                log(f"autotune {c}: {results[c]:.2f} ms")
+                torch.cuda.synchronize()
+                t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                t0.record()
+                for _ in range(reps):
+                    target.launch()
+                t1.record()
+                torch.cuda.synchronize()
+                k = tuple(c) + ((scale,) if scale is not None else ())
+                results[k] = t0.elapsed_time(t1) / reps
+                if log:
+                    log(f"autotune {k}: {results[k]:.2f} ms")
         st, flags = P.device_errors()
         if st != 0 or flags != 0:
             raise LyemError(st or 2, f"batch autotune: device error word {flags:#x}")
         best = min(results, key=results.get)
-        self.configure(best)
+        self.config = best[:3]
+        if len(best) == 4:
+            self.set_cell_scale(best[3])
+        else:
+            self.configure(best[:3])
         if use_cache:
             cache[key] = {"config": list(best), "ms": results[best]}
             try:

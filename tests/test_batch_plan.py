@@ -78,3 +78,15 @@ def test_rejects_bad_arguments():
     assert lib.lyem_batch_workspace(bad, 1, 100, 16, ctypes.byref(_cfg())) == 0
     assert lib.lyem_batch_workspace(scenes, 0, 100, 16, ctypes.byref(_cfg())) == 0
     assert lib.lyem_batch_items(scenes, 1, 0, 16, ctypes.byref(_cfg()), None) < 0
+
+
+def test_density_cell():
+    from lyceanem_gb300.batched import density_cell
+    # 10 x 10 x 1 m box, 1000 triangles: 0.1 m^3 per triangle
+    c = density_cell([0, 0, 0, 10, 10, 1], 1000, 1.0)
+    assert abs(c - 0.1 ** (1 / 3)) < 1e-12
+    assert abs(density_cell([0, 0, 0, 10, 10, 1], 1000, 2.0) - 2 * c) < 1e-12
+    # flat box: the thin axis counts as 1 mm, and the result is clipped to [0.05, 10] m
+    assert density_cell([0, 0, 0, 1, 1, 0], 10 ** 6, 1.0) == 0.05
+    assert density_cell([0, 0, 0, 1e3, 1e3, 1e3], 1, 1.0) == 10.0
+    assert density_cell([0, 0, 0, 1, 1, 1], 0, 1.0) == 1.0

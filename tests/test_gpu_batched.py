@@ -182,3 +182,32 @@ def test_autotune_picks_and_caches(small, tmp_path, monkeypatch):
     assert list(cached) == [bs.config] and again.config == bs.config
     assert _check(again.run().cpu().numpy(), ref) < FIELD_TOL
     assert P.device_errors() == (0, 0)
+
+
+def test_density_cells_same_field(small, tmp_path, monkeypatch):
+    """Density-scaled grids (one scale for the batch, a cell per scene) change only the traversal
+    work: the same visible paths and fields as the oracle; the autotuner picks a scale."""
+    B, P, _ = _mods()
+    scenes, snk, snk_n, freqs, ref, counts = small
+    tests = []
+    for k in (0.6, 1.0, 1.7):
+        bs = B.BatchedScattering(scenes, snk, snk_n, freqs, config=(2, 64, 0), cell_scale=k)
+        cells = bs.grid_cells()
+        assert len(set(round(c, 6) for c in cells)) > 1  # scenes of different density get different cells
+        field = bs.run().cpu().numpy()
+        assert _check(field, ref) < FIELD_TOL, f"scale {k}"
+        cnt = bs.counters.cpu().numpy()
+        assert np.array_equal(cnt[:, :3], counts), f"scale {k}"
+        tests.append(int(cnt[:, 3].sum()))
+    assert tests[0] != tests[2]
+    monkeypatch.setenv("LYEM_TUNE_CACHE", str(tmp_path / "tune.json"))
+    bs = B.BatchedScattering(scenes, snk, snk_n, freqs)
+    res = bs.autotune(candidates=[(2, 64, 0), (4, 32, 4)], cell_scales=[0.8, 1.2])
+    assert len(res) == 4 and all(len(k) == 4 for k in res)
+    best = min(res, key=res.get)
+    assert bs.config + (bs.cell_scale,) == best
+    assert _check(bs.run().cpu().numpy(), ref) < FIELD_TOL
+    again = B.BatchedScattering(scenes, snk, snk_n, freqs)
+    cached = again.autotune(candidates=[(2, 64, 0), (4, 32, 4)], cell_scales=[0.8, 1.2])
+    assert list(cached) == [best] and again.cell_scale == best[3] and again.grid_cells() == bs.grid_cells()
+    assert P.device_errors() == (0, 0)
