@@ -89,6 +89,42 @@ def test_grid_and_brute_masks_bit_exact(seed):
     _no_device_errors()
 
 
+@pytest.mark.parametrize("eps", [1e-6, 0.0])
+def test_grazing_rays_masks_bit_exact(eps):
+    """Rays nearly in the planes of the triangles (determinant near zero, both windings, triangle sizes
+    1e-3 to 0.3 m, plane tilts 1e-8 to 1e-1): culled masks of the grid walk and of the brute-force kernel
+    bit-exact to the oracle."""
+    P = _P()
+    rng = np.random.default_rng(21)
+    n_t = 600
+    size = 10.0 ** rng.uniform(-3, -0.5, n_t)
+    tilt = 10.0 ** rng.uniform(-8, -1, n_t) * rng.choice([-1.0, 1.0], n_t)
+    centre = rng.uniform(-1, 1, (n_t, 3)) * np.array([2.0, 1.0, 0.05])
+    verts = []
+    for k in range(n_t):
+        a = rng.uniform(-1, 1, (3, 2)) * size[k]
+        pts = centre[k] + np.stack([a[:, 0], a[:, 1], tilt[k] * a[:, 0]], 1)
+        verts.append(pts[::-1] if rng.random() < 0.5 else pts)
+    v = np.concatenate(verts).astype(np.float32)
+    f = np.arange(3 * n_t, dtype=np.int32).reshape(-1, 3)
+    n_src, n_snk = 40, 256
+    src = np.stack([np.full(n_src, -3.0), rng.uniform(-1, 1, n_src), rng.uniform(-0.05, 0.05, n_src)], 1)
+    snk = np.stack([np.full(n_snk, 3.0), rng.uniform(-1, 1, n_snk), rng.uniform(-0.05, 0.05, n_snk)], 1)
+    src, snk = src.astype(np.float32), snk.astype(np.float32)
+    snk_n = np.tile(np.array([[-1.0, 0.0, 0.0]], np.float32), (n_snk, 1))
+    E = np.tile(np.array([[1, 0, 0]], np.complex64), (n_src, 1))
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f), cull=True, eps=eps)
+    assert 0 < om.sum() < om.size
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    rb = P.pair_stage(src, E, snk, snk_n, beta=10.0, tris=tris, eps=eps, want_mask=True)
+    assert np.array_equal(rb.mask().cpu().numpy(), om)
+    for cell in (0.05, 0.5):
+        g = P.UniformGrid(tris, cell=cell)
+        r = P.pair_stage(src, E, snk, snk_n, beta=10.0, grid=g, eps=eps, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), om), cell
+    _no_device_errors()
+
+
 def test_grid_build_matches_cpu_binning():
     """Cell ranges of the device grid equal a NumPy restatement of the padded-box binning."""
     P = _P()
