@@ -99,15 +99,20 @@ LYEM_API int lyem_grid_count(const float *d_tris, int64_t n_tris, const float *o
 
 /* Uniform-grid build, phase 2: emits (cell, triangle) keys, radix-sorts them
  * by cell (stable, so triangles are ascending within a cell), writes the cell
- * ranges d_cell_start[ncells+1] and the triangles in cell order
- * d_cell_tris[n_refs,12].  Replaces bin_triangles_kernel_precounted /
+ * ranges d_cell_start[ncells+1], the triangles in cell order
+ * d_cell_tris[n_refs,12] and the traversal's cell table d_cell_box[ncells,8]
+ * (16-byte aligned): per cell (lo.x, lo.y, lo.z, first ref, hi.x, hi.y, hi.z,
+ * end ref), the refs stored as int32 bits and [lo, hi] the box of the cell's
+ * triangles (padded as for the binning) within the cell widened by two pads;
+ * a segment that misses it skips the cell's triangles.  Replaces bin_triangles_kernel_precounted /
  * compute_bin_offsets / insert_triangle_in_bin
  * (lyceanem/src/terrain_acceleration_build.cuh:135-205, 349-368) and the host
  * prefix sum of lyceanem/src/frequency_domain_models.cu:118-123. */
 LYEM_API size_t lyem_grid_fill_workspace(int64_t n_refs, int64_t n_cells);
 LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *origin3, float cell,
                             const int32_t *dims3, const int32_t *d_tri_offsets, int64_t n_refs,
-                            int32_t *d_cell_start, float *d_cell_tris, void *d_ws, size_t ws_bytes, void *stream);
+                            int32_t *d_cell_start, float *d_cell_tris, float *d_cell_box, void *d_ws, size_t ws_bytes,
+                            void *stream);
 
 /* Spatial (Morton / Z-order) order of a point set: d_order[n_points] lists the
  * point indices so that consecutive entries are close in space.  Passed to
@@ -126,7 +131,7 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * lyceanem/src/raycasting.cuh:19-68 (cull = 1) or the numba engine's
  * lyceanem/raycasting/rayfunctions.py:37-104 (cull = 0, eps = 1e-7) against all
  * packed triangles (brute force, d_cell_start == NULL) or a grid from
- * lyem_grid_fill.  self_to_self = 0 reproduces the reference's skip of the pair
+ * lyem_grid_fill (d_cell_start, d_cell_tris and d_cell_box all given).  self_to_self = 0 reproduces the reference's skip of the pair
  * whose source index equals its sink index (lyceanem/src/raycasting_brute_force.cuh:27).
  * Replaces raycast_brute_force / raycast_tiles + set_values + points_to_rays
  * (lyceanem/src/raycasting_brute_force.cuh:68-88, raycasting_accelerated.cuh:458-482,
@@ -154,8 +159,9 @@ LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t 
 LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const float *d_src_W, int64_t n_src,
                              const float *d_snk_pos, const float *d_snk_nrm, int64_t n_snk, const float *d_tris,
                              int64_t n_tris, const int32_t *d_cell_start, const float *d_cell_tris,
-                             const float *grid_origin3, float grid_cell, const int32_t *grid_dims3, double alpha,
-                             double beta, int32_t self_to_self, int32_t cull, float eps, float *d_sink_out,
+                             const float *d_cell_box, const float *grid_origin3, float grid_cell,
+                             const int32_t *grid_dims3, double alpha, double beta, int32_t self_to_self, int32_t cull,
+                             float eps, float *d_sink_out,
                              int32_t accumulate, float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
                              int32_t *d_src_visible, int32_t *d_snk_visible, const int32_t *d_src_order,
                              const int32_t *d_snk_order, int32_t src_chunk, int32_t traversal, void *d_ws,
@@ -179,7 +185,8 @@ LYEM_API size_t lyem_pair_stage_noalloc_scratch_bytes(void);
 LYEM_API int lyem_pair_stage_noalloc(const float *d_src_pos, const float *d_src_E, const float *d_src_W,
                                      int64_t n_src, const float *d_snk_pos, const float *d_snk_nrm, int64_t n_snk,
                                      const float *d_tris, int64_t n_tris, const int32_t *d_cell_start,
-                                     const float *d_cell_tris, const float *grid_origin3, float grid_cell,
+                                     const float *d_cell_tris, const float *d_cell_box, const float *grid_origin3,
+                                     float grid_cell,
                                      const int32_t *grid_dims3, double alpha, double beta, int32_t self_to_self,
                                      int32_t cull, float eps, float *d_sink_out, int32_t accumulate,
                                      float *d_pair_out, uint32_t *d_mask_bits, uint64_t *d_counters,
@@ -258,6 +265,7 @@ typedef struct lyem_batch_scene {
     const int32_t *scat_id;    /* [n_scat] or NULL */
     const int32_t *cell_start; /* [cells + 1] */
     const float *cell_tris;    /* [refs, 12], 16-byte aligned */
+    const float *cell_box;     /* [cells, 8], 16-byte aligned (lyem_grid_fill) */
     int64_t n_src;
     int64_t n_scat;
     float grid_origin[3];

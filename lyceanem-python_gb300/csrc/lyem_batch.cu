@@ -64,6 +64,7 @@ enum Kind { kVisScat = 0, kVisDirect = 1, kVisBounce = 2, kFieldW = 3, kFieldE =
 struct GridView {
     const int* cell_start;
     const float4* cell_tris;
+    const float4* cell_box;
     float g0[3], g1[3];
     float cell, inv_cell;
     int dims[3];
@@ -533,7 +534,8 @@ int make_plan(const lyem_batch_scene* sc, int n_scenes, long long n_snk, int n_f
         if (N < 0 || P < 0 || N >= (1LL << 31) || P >= (1LL << 31)) return LYEM_ERR_INVALID;
         if (N > 0 && (!sc[s].src_pos || !sc[s].src_E)) return LYEM_ERR_INVALID;
         if (P > 0 && (!sc[s].scat_pos || !sc[s].scat_nrm)) return LYEM_ERR_INVALID;
-        if (!sc[s].cell_start || !sc[s].cell_tris || (reinterpret_cast<uintptr_t>(sc[s].cell_tris) & 15u))
+        if (!sc[s].cell_start || !sc[s].cell_tris || (reinterpret_cast<uintptr_t>(sc[s].cell_tris) & 15u) ||
+            !sc[s].cell_box || (reinterpret_cast<uintptr_t>(sc[s].cell_box) & 15u))
             return LYEM_ERR_INVALID;
         long long nc = 1;
         for (int k = 0; k < 3; ++k) {
@@ -724,6 +726,7 @@ LYEM_API int lyem_batch_prepare(const lyem_batch_scene* scenes, int32_t n_scenes
         d.n_scat = c.n_scat;
         d.grid.cell_start = c.cell_start;
         d.grid.cell_tris = reinterpret_cast<const float4*>(c.cell_tris);
+        d.grid.cell_box = reinterpret_cast<const float4*>(c.cell_box);
         for (int k = 0; k < 3; ++k) {
             d.grid.g0[k] = c.grid_origin[k];
             d.grid.g1[k] = c.grid_origin[k] + c.grid_dims[k] * c.grid_cell;

@@ -251,16 +251,18 @@ LYEM_API size_t lyem_grid_fill_workspace(int64_t n_refs, int64_t n_cells) {
 
 LYEM_API int lyem_grid_fill(const float* d_tris, int64_t n_tris, const float* origin3, float cell,
                             const int32_t* dims3, const int32_t* d_tri_offsets, int64_t n_refs, int32_t* d_cell_start,
-                            float* d_cell_tris, void* d_ws, size_t ws_bytes, void* stream) {
+                            float* d_cell_tris, float* d_cell_box, void* d_ws, size_t ws_bytes, void* stream) {
     if (n_tris < 0 || n_refs < 0 || !d_tri_offsets || !d_cell_start || !valid_grid(origin3, cell, dims3))
         return LYEM_ERR_INVALID;
+    if (!d_cell_box || !aligned16(d_cell_box)) return LYEM_ERR_INVALID;
     if (n_refs > 0 && (!d_cell_tris || !aligned16(d_cell_tris) || !d_tris || !aligned16(d_tris))) return LYEM_ERR_INVALID;
     if (n_refs >= (1LL << 31) - 64) return LYEM_ERR_OVERFLOW;
     const long long ncells = (long long)dims3[0] * dims3[1] * dims3[2];
     if (!d_ws || ws_bytes < grid_fill_workspace_bytes(n_refs, ncells)) return LYEM_ERR_WORKSPACE;
     BinSpec b = grid_spec(origin3, cell, dims3);
     LYEM_CK(grid_fill(b, reinterpret_cast<const float4*>(d_tris), n_tris, d_tri_offsets, n_refs, d_cell_start,
-                      reinterpret_cast<float4*>(d_cell_tris), d_ws, as_stream(stream)));
+                      reinterpret_cast<float4*>(d_cell_tris), reinterpret_cast<float4*>(d_cell_box), d_ws,
+                      as_stream(stream)));
     return LYEM_OK;
 }
 
@@ -291,8 +293,9 @@ LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t 
 LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const float* d_src_W, int64_t n_src,
                              const float* d_snk_pos, const float* d_snk_nrm, int64_t n_snk, const float* d_tris,
                              int64_t n_tris, const int32_t* d_cell_start, const float* d_cell_tris,
-                             const float* grid_origin3, float grid_cell, const int32_t* grid_dims3, double alpha,
-                             double beta, int32_t self_to_self, int32_t cull, float eps, float* d_sink_out,
+                             const float* d_cell_box, const float* grid_origin3, float grid_cell,
+                             const int32_t* grid_dims3, double alpha, double beta, int32_t self_to_self, int32_t cull,
+                             float eps, float* d_sink_out,
                              int32_t accumulate, float* d_pair_out, uint32_t* d_mask_bits, uint64_t* d_counters,
                              int32_t* d_src_visible, int32_t* d_snk_visible, const int32_t* d_src_order,
                              const int32_t* d_snk_order, int32_t src_chunk, int32_t traversal, void* d_ws,
@@ -307,7 +310,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     if (!d_src_pos || !d_src_E || !d_snk_pos || !d_snk_nrm) return LYEM_ERR_INVALID;
     if (n_src > (1LL << 31) || n_snk > (1LL << 31)) return LYEM_ERR_OVERFLOW;
     if (use_grid) {
-        if (!d_cell_tris || !aligned16(d_cell_tris) || !valid_grid(grid_origin3, grid_cell, grid_dims3))
+        if (!d_cell_tris || !aligned16(d_cell_tris) || !d_cell_box || !aligned16(d_cell_box) ||
+            !valid_grid(grid_origin3, grid_cell, grid_dims3))
             return LYEM_ERR_INVALID;
     } else if (n_tris > 0 && (!d_tris || !aligned16(d_tris))) {
         return LYEM_ERR_INVALID;
@@ -335,6 +339,7 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     if (use_grid) {
         p.cell_start = d_cell_start;
         p.cell_tris = reinterpret_cast<const float4*>(d_cell_tris);
+        p.cell_box = reinterpret_cast<const float4*>(d_cell_box);
         for (int k = 0; k < 3; ++k) {
             p.g0[k] = grid_origin3[k];
             p.g1[k] = grid_origin3[k] + grid_dims3[k] * grid_cell;
@@ -500,7 +505,7 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
     const size_t pair_bytes = 24 * (size_t)n_source * (size_t)n_end;
     LYEM_CK(dpair.alloc(pair_bytes, s));
 
-    DevBuf dstart, dcell, dws;
+    DevBuf dstart, dcell, dbox, dws;
     float org[3] = {0, 0, 0}, cell = 1.f;
     int32_t dims[3] = {1, 1, 1};
     if (use_grid && n_tris > 0) {
@@ -524,17 +529,19 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
         const long long ncells = (long long)dims[0] * dims[1] * dims[2];
         LYEM_CK(dstart.alloc(sizeof(int) * (size_t)(ncells + 1), s));
         LYEM_CK(dcell.alloc(48 * (size_t)total, s));
+        LYEM_CK(dbox.alloc(32 * (size_t)ncells, s));
         DevBuf dfw;
         LYEM_CK(dfw.alloc(grid_fill_workspace_bytes((long long)total, ncells), s));
         LYEM_CK(grid_fill(b, dt.as<float4>(), n_tris, doff.as<int>(), (long long)total, dstart.as<int>(),
-                          dcell.as<float4>(), dfw.p, s));
+                          dcell.as<float4>(), dbox.as<float4>(), dfw.p, s));
     }
     const bool grid_on = use_grid && n_tris > 0;
     const size_t ws = lyem_pair_stage_workspace(n_source, n_end, n_tris, grid_on, 0);
     LYEM_CK(dws.alloc(ws, s));
     int st = lyem_pair_stage(dsrc.as<float>(), dE.as<float>(), nullptr, n_source, dend.as<float>(), dnrm.as<float>(),
                              n_end, dt.as<float>(), n_tris, grid_on ? dstart.as<int32_t>() : nullptr,
-                             grid_on ? dcell.as<float>() : nullptr, org, cell, dims, (double)alpha, (double)beta,
+                             grid_on ? dcell.as<float>() : nullptr, grid_on ? dbox.as<float>() : nullptr, org, cell,
+                             dims, (double)alpha, (double)beta,
                              not_self_to_self, 1, kEpsilon, nullptr, 0, dpair.as<float>(), nullptr, nullptr, nullptr,
                              nullptr, nullptr, nullptr, 0, 0, dws.p, ws, s);
     if (st != LYEM_OK) return st;

@@ -9,7 +9,9 @@
 //      triangles of a cell stay in ascending order and the build is deterministic;
 //   5. cell ranges by binary search of the sorted keys;
 //   6. gather the packed triangles into cell order (contiguous float4 loads
-//      for the traversal).
+//      for the traversal);
+//   7. per cell, the box of its triangles within the cell and its ref range
+//      (one 32-byte record per cell step of the traversal).
 // This replaces the reference's vertex binning with device asserts, its
 // O(cells^2) single-block offset computation and its atomicCAS slot
 // insertion (lyceanem/src/terrain_acceleration_build.cuh:30-205, 287-431) and
@@ -326,6 +328,45 @@ __global__ void gather_tris_kernel(const float4* __restrict__ tris, const int* _
     }
 }
 
+// Cell table of the traversal: for cell c the union of the padded boxes of its
+// triangles (vertices and pad exactly as covered_range computes them), clipped
+// to the cell widened by two pads, and the cell's ref range.  A segment whose
+// exact path misses this box cannot hit a triangle of the cell inside the cell
+// (a hit point lies in its triangle's box and in the cell, at least a pad inside
+// the clipped box), and a hit outside the cell is found in the cell that holds it.
+// Empty cells get lo = +inf, hi = -inf.  Non-finite triangle coordinates are
+// ignored by fminf/fmaxf: such triangles never pass the ray-triangle test.
+__global__ void cell_box_kernel(BinSpec b, const int* __restrict__ cell_start, const float4* __restrict__ cell_tris,
+                                long long ncells, float4* __restrict__ box) {
+    const long long plane = (long long)b.dims[0] * b.dims[1];
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncells;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int q0 = cell_start[c], q1 = cell_start[c + 1];
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int r = q0; r < q1; ++r) {
+            const float4 v0 = cell_tris[3 * (long long)r], e1 = cell_tris[3 * (long long)r + 1],
+                         e2 = cell_tris[3 * (long long)r + 2];
+            const float a[3] = {v0.x, v0.y, v0.z}, e[3] = {e1.x, e1.y, e1.z}, f[3] = {e2.x, e2.y, e2.z};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float p = a[k], q = a[k] + e[k], s = a[k] + f[k];
+                lo[k] = fminf(lo[k], fminf(p, fminf(q, s)) - b.pad);
+                hi[k] = fmaxf(hi[k], fmaxf(p, fmaxf(q, s)) + b.pad);
+            }
+        }
+        const long long iz = c / plane, rem = c - iz * plane, iy = rem / b.dims[0], ix = rem - iy * b.dims[0];
+        const float ci[3] = {(float)ix, (float)iy, (float)iz};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float c0 = b.org[k] + ci[k] * b.cell;
+            lo[k] = fmaxf(lo[k], c0 - 2.f * b.pad);
+            hi[k] = fminf(hi[k], c0 + b.cell + 2.f * b.pad);
+        }
+        box[2 * c] = make_float4(lo[0], lo[1], lo[2], __int_as_float(q0));
+        box[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q1));
+    }
+}
+
 __global__ void gather_index_kernel(const int* __restrict__ tri_index, const int* __restrict__ vals, long long n,
                                     int* out) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * n;
@@ -488,11 +529,16 @@ cudaError_t grid_sort(const BinSpec& b, const float4* tris, long long n_tris, co
 }
 
 cudaError_t grid_fill(const BinSpec& b, const float4* tris, long long n_tris, const int* tri_offsets, long long n_refs,
-                      int* cell_start, float4* cell_tris, void* ws, cudaStream_t stream) {
+                      int* cell_start, float4* cell_tris, float4* cell_box, void* ws, cudaStream_t stream) {
     const int* vals = nullptr;
     cudaError_t e = grid_sort(b, tris, n_tris, tri_offsets, n_refs, cell_start, &vals, ws, stream);
     if (e != cudaSuccess) return e;
     if (n_refs > 0) { gather_tris_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tris, vals, n_refs, cell_tris); note_launches(1); }
+    if (cell_box) {
+        const long long ncells = (long long)b.dims[0] * b.dims[1] * b.dims[2];
+        cell_box_kernel<<<grid_blocks(ncells, 256), 256, 0, stream>>>(b, cell_start, cell_tris, ncells, cell_box);
+        note_launches(1);
+    }
     return cudaGetLastError();
 }
 

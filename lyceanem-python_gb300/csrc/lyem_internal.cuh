@@ -36,6 +36,7 @@ struct StageParams {
     // uniform grid (used when cell_start != nullptr)
     const int* cell_start;     // [ncells + 1]
     const float4* cell_tris;   // [n_refs, 3] float4, triangles in cell order
+    const float4* cell_box;    // [ncells, 2] float4: box of the cell's triangles and ref range
     float g0[3], g1[3];        // grid box
     float cell, inv_cell;
     int dims[3];

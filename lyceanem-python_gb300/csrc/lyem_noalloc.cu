@@ -58,7 +58,8 @@ LYEM_API size_t lyem_pair_stage_noalloc_scratch_bytes(void) { return kNoallocScr
 LYEM_API int lyem_pair_stage_noalloc(const float* d_src_pos, const float* d_src_E, const float* d_src_W,
                                      int64_t n_src, const float* d_snk_pos, const float* d_snk_nrm, int64_t n_snk,
                                      const float* d_tris, int64_t n_tris, const int32_t* d_cell_start,
-                                     const float* d_cell_tris, const float* grid_origin3, float grid_cell,
+                                     const float* d_cell_tris, const float* d_cell_box, const float* grid_origin3,
+                                     float grid_cell,
                                      const int32_t* grid_dims3, double alpha, double beta, int32_t self_to_self,
                                      int32_t cull, float eps, float* d_sink_out, int32_t accumulate,
                                      float* d_pair_out, uint32_t* d_mask_bits, uint64_t* d_counters,
@@ -89,7 +90,8 @@ LYEM_API int lyem_pair_stage_noalloc(const float* d_src_pos, const float* d_src_
     int st = scratch_address(&scratch);
     if (st != LYEM_OK) return st;
     return lyem_pair_stage(d_src_pos, d_src_E, d_src_W, n_src, d_snk_pos, d_snk_nrm, n_snk, d_tris, n_tris,
-                           d_cell_start, d_cell_tris, grid_origin3, grid_cell, grid_dims3, alpha, beta, self_to_self,
+                           d_cell_start, d_cell_tris, d_cell_box, grid_origin3, grid_cell, grid_dims3, alpha, beta,
+                           self_to_self,
                            cull, eps, d_sink_out, accumulate, d_pair_out, d_mask_bits, d_counters, d_src_visible,
                            d_snk_visible, d_src_order, d_snk_order, chunk, traversal, scratch, kNoallocScratchBytes,
                            stream);

@@ -2,8 +2,10 @@
 // by the pair-stage kernels (lyem_stage.cu) and the batched kernel (lyem_batch.cu).
 // Amanatides-Woo; boundary crossings are recomputed from the cell index, so no
 // error accumulates; triangles are stored contiguously per cell (float4 loads).
+// Entering a cell reads its 32-byte record (box of its triangles, ref range)
+// and skips the cell's triangles when the segment misses the box.
 // GP is any parameter block with the grid fields of StageParams (g0, g1, cell,
-// inv_cell, dims, cell_start, cell_tris, eps).
+// inv_cell, dims, cell_box, cell_tris, eps).
 #pragma once
 #include "lyem_device.cuh"
 #include "lyem_internal.cuh"
@@ -16,6 +18,37 @@ struct Walk {
     float ix, iy, iz, t1;
     int cx, cy, cz, q, q1, guard;
 };
+
+// Enters cell c: its ref range, emptied when the segment misses the box of
+// the cell's triangles.  Slab test over the parameter range [0, len] (the
+// cell's own range is a part of it); an axis the segment is parallel to only
+// checks the origin coordinate.  The computed slab parameters carry relative
+// errors of a few units of 2^-24, so the box counts as missed only when the
+// entry parameter exceeds the exit parameter by more than 2^-19 of it; NaN
+// parameters never make a miss.
+template <class GP>
+__device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
+    const float4 lo = __ldg(p.cell_box + 2 * (long long)c), hi = __ldg(p.cell_box + 2 * (long long)c + 1);
+    w.q = __float_as_int(lo.w);
+    w.q1 = __float_as_int(hi.w);
+    if (w.q >= w.q1) return;
+    const float kInf = __int_as_float(0x7f800000);
+    float tmin = 0.f, tmax = w.r.len;
+    bool out = false;
+#define LYEM_BOX(D, O, INV, L, H)                                     \
+    {                                                                 \
+        const float ta = D != 0.f ? (L - O) * INV : -kInf;            \
+        const float tb = D != 0.f ? (H - O) * INV : kInf;             \
+        tmin = fmaxf(tmin, fminf(ta, tb));                            \
+        tmax = fminf(tmax, fmaxf(ta, tb));                            \
+        out |= D == 0.f && (O < L || O > H);                          \
+    }
+    LYEM_BOX(w.r.dx, w.ox, w.ix, lo.x, hi.x)
+    LYEM_BOX(w.r.dy, w.oy, w.iy, lo.y, hi.y)
+    LYEM_BOX(w.r.dz, w.oz, w.iz, lo.z, hi.z)
+#undef LYEM_BOX
+    if (out || __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax) w.q = w.q1;
+}
 
 // Starts the walk of segment o -> e; false if the segment misses the grid box.
 template <class GP>
@@ -45,9 +78,7 @@ __device__ __forceinline__ bool walk_begin(const GP& p, Walk& w, float ox, float
     w.cy = min(max((int)floorf((oy + t0 * w.r.dy - p.g0[1]) * p.inv_cell), 0), p.dims[1] - 1);
     w.cz = min(max((int)floorf((oz + t0 * w.r.dz - p.g0[2]) * p.inv_cell), 0), p.dims[2] - 1);
     w.guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
-    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
-    w.q = __ldg(p.cell_start + c);
-    w.q1 = __ldg(p.cell_start + c + 1);
+    walk_enter(p, w, (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx);
     return true;
 }
 
@@ -87,9 +118,7 @@ __device__ __forceinline__ bool walk_step(const GP& p, Walk& w, unsigned int* er
         done = true;
     }
     if (done) return false;
-    const int c = (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx;
-    w.q = __ldg(p.cell_start + c);
-    w.q1 = __ldg(p.cell_start + c + 1);
+    walk_enter(p, w, (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx);
     return true;
 }
 

@@ -46,7 +46,7 @@ _u32p = ctypes.POINTER(ctypes.c_uint32)
 class BatchScene(ctypes.Structure):
     """lyem_batch_scene of include/lyem.h (device pointers and sizes of one scene)."""
     _fields_ = [("src_pos", _vp), ("src_E", _vp), ("scat_pos", _vp), ("scat_nrm", _vp), ("scat_id", _vp),
-                ("cell_start", _vp), ("cell_tris", _vp), ("n_src", _i64), ("n_scat", _i64),
+                ("cell_start", _vp), ("cell_tris", _vp), ("cell_box", _vp), ("n_src", _i64), ("n_scat", _i64),
                 ("grid_origin", _f32 * 3), ("grid_cell", _f32), ("grid_dims", _i32 * 3), ("reserved", _i32)]
 
 
@@ -75,16 +75,16 @@ SIGNATURES = {
     "lyem_grid_count_workspace": ([_i64], _sz),
     "lyem_grid_count": ([_vp, _i64, _f32p, _f32, _i32p, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_grid_fill_workspace": ([_i64, _i64], _sz),
-    "lyem_grid_fill": ([_vp, _i64, _f32p, _f32, _i32p, _vp, _i64, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "lyem_grid_fill": ([_vp, _i64, _f32p, _f32, _i32p, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_spatial_order_workspace": ([_i64], _sz),
     "lyem_spatial_order": ([_vp, _i64, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_pair_stage_workspace": ([_i64, _i64, _i64, _i32, _i32], _sz),
-    "lyem_pair_stage": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _f32p, _f32, _i32p, _f64, _f64,
+    "lyem_pair_stage": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _f32p, _f32, _i32p, _f64, _f64,
                          _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _sz,
                          _vp],
                         ctypes.c_int),
     "lyem_pair_stage_noalloc_scratch_bytes": ([], _sz),
-    "lyem_pair_stage_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _f32p, _f32, _i32p, _f64,
+    "lyem_pair_stage_noalloc": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _f32p, _f32, _i32p, _f64,
                                  _f64, _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32,
                                  _vp], ctypes.c_int),
     "lyem_mask_to_bytes": ([_vp, _i64, _i64, _vp, _vp], ctypes.c_int),

@@ -115,6 +115,7 @@ class _SceneData:
         b.scat_id = self.scat_id.data_ptr() if self.scat.shape[0] else None
         b.cell_start = g.cell_start.data_ptr()
         b.cell_tris = g.cell_tris.data_ptr()
+        b.cell_box = g.cell_box.data_ptr()
         b.n_src = self.src.shape[0]
         b.n_scat = self.scat.shape[0]
         for k in range(3):

@@ -103,10 +103,12 @@ class UniformGrid:
         ncells = self.dims[0] * self.dims[1] * self.dims[2]
         self.cell_start = torch.empty(ncells + 1, dtype=torch.int32, device=dev)
         self.cell_tris = torch.empty((max(self.n_refs, 1), 12), dtype=torch.float32, device=dev)
+        # per cell: (lo.xyz, first ref) (hi.xyz, end ref), the box of the cell's triangles
+        self.cell_box = torch.empty((ncells, 8), dtype=torch.float32, device=dev)
         ws2 = _ws(lib.lyem_grid_fill_workspace(self.n_refs, ncells), dev)
         check(lib.lyem_grid_fill(_p(tris), T, f32arr(self.origin), self.cell, i32arr(self.dims), _p(offsets),
-                                 self.n_refs, _p(self.cell_start), _p(self.cell_tris), _p(ws2), ws2.numel(),
-                                 _stream()), "grid_fill")
+                                 self.n_refs, _p(self.cell_start), _p(self.cell_tris), _p(self.cell_box), _p(ws2),
+                                 ws2.numel(), _stream()), "grid_fill")
         self._org_c = f32arr(self.origin)
         self._dims_c = i32arr(self.dims)
 
@@ -159,12 +161,13 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     M = tp.shape[0]
     if grid is not None:
         tri_t, T = None, 0
-        cs, ct, org, cell, dims = grid.cell_start, grid.cell_tris, grid._org_c, grid.cell, grid._dims_c
+        cs, ct, cb = grid.cell_start, grid.cell_tris, grid.cell_box
+        org, cell, dims = grid._org_c, grid.cell, grid._dims_c
     else:
         tri_t = _dev(tris, torch.float32).reshape(-1, 12).contiguous() if tris is not None else \
             torch.zeros((0, 12), dtype=torch.float32, device=dev)
         T = tri_t.shape[0]
-        cs = ct = None
+        cs = ct = cb = None
         org, cell, dims = f32arr([0, 0, 0]), 1.0, i32arr([1, 1, 1])
     if sink_out is None:
         sink_out = torch.empty((M, 3), dtype=torch.complex64, device=dev)
@@ -176,7 +179,8 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     if workspace is None or workspace.numel() < need:
         workspace = _ws(need, dev)
     st = lib.lyem_pair_stage(_p(sp), _p(torch.view_as_real(E)), _p(None if W is None else torch.view_as_real(W)), N,
-                             _p(tp), _p(tn), M, _p(tri_t), T, _p(cs), _p(ct), org, float(cell), dims, float(alpha),
+                             _p(tp), _p(tn), M, _p(tri_t), T, _p(cs), _p(ct), _p(cb), org, float(cell), dims,
+                             float(alpha),
                              float(beta), int(bool(self_to_self)), int(bool(cull)), float(eps),
                              _p(torch.view_as_real(sink_out)), int(bool(accumulate)),
                              _p(None if pairs is None else torch.view_as_real(pairs)), _p(mbits), _p(counters),

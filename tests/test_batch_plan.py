@@ -14,7 +14,7 @@ def _scene(n_src, n_scat, dims=(4, 4, 4)):
     s.src_pos = s.src_E = FAKE
     s.scat_pos = s.scat_nrm = FAKE if n_scat else None
     s.scat_id = None
-    s.cell_start = s.cell_tris = FAKE
+    s.cell_start = s.cell_tris = s.cell_box = FAKE
     s.n_src, s.n_scat = n_src, n_scat
     for k in range(3):
         s.grid_origin[k] = -1.0

@@ -149,6 +149,20 @@ def test_grid_build_matches_cpu_binning():
     for c in range(g.n_cells):
         got = ct[start[c]:start[c + 1]]
         assert np.array_equal(got, t[cells[c]]), c
+    # cell table: ref range and the box of the cell's padded triangle boxes within the cell widened by 2 pads
+    box = g.cell_box.cpu().numpy()
+    refs = np.ascontiguousarray(box[:, [3, 7]]).view(np.int32)
+    assert np.array_equal(refs[:, 0], start[:-1]) and np.array_equal(refs[:, 1], start[1:])
+    pad = np.float32(1e-3) * np.float32(g.cell)
+    vlo, vhi = vv.min(1) - pad, vv.max(1) + pad
+    for c in range(g.n_cells):
+        if not cells[c]:
+            continue
+        ix = np.array([c % g.dims[0], (c // g.dims[0]) % g.dims[1], c // (g.dims[0] * g.dims[1])])
+        c0 = org + ix * np.float32(g.cell)
+        lo = np.maximum(vlo[cells[c]].min(0), c0 - 2 * pad)
+        hi = np.minimum(vhi[cells[c]].max(0), c0 + np.float32(g.cell) + 2 * pad)
+        assert np.allclose(box[c, 0:3], lo, rtol=0, atol=1e-5) and np.allclose(box[c, 4:7], hi, rtol=0, atol=1e-5), c
 
 
 def test_bounce_scene_reduced_vs_oracle():

@@ -38,10 +38,11 @@ def _args(src, E, snk, snk_n, tris, grid):
     """Common leading arguments of both entry points (device tensors, brute force or grid)."""
     from lyceanem_gb300._native import f32arr, i32arr
     if grid is None:
-        g = (None, None, f32arr([0, 0, 0]), 1.0, i32arr([1, 1, 1]))
+        g = (None, None, None, f32arr([0, 0, 0]), 1.0, i32arr([1, 1, 1]))
         t, T = tris, tris.shape[0]
     else:
-        g = (_p(grid.cell_start), _p(grid.cell_tris), f32arr(grid.origin), grid.cell, i32arr(grid.dims))
+        g = (_p(grid.cell_start), _p(grid.cell_tris), _p(grid.cell_box), f32arr(grid.origin), grid.cell,
+             i32arr(grid.dims))
         t, T = None, 0
     return [_p(src), _p(torch.view_as_real(E)), None, src.shape[0], _p(snk), _p(snk_n), snk.shape[0], _p(t), T, *g]
 
