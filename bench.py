@@ -35,9 +35,9 @@ METRIC = "visible paths/s (mask+field) on 1 GB300; mixed-prec vs FP32 sweep at â
 OPS_PER_TEST = 30  # FP32-pipe operations of one Moller-Trumbore test (lyceanem/src/raycasting.cuh:23-59)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one full-size launch of the scatter->sink grid-stage kernel, from the
-# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (117.02 MB + 4.88 GB; the
-# writes are the per-chunk partial sums).
-GRID_STAGE_DRAM_BYTES = 117.02e6 + 4.88e9
+# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (213.85 MB + 5.87 GB; the
+# writes are mostly the per-chunk partial sums).
+GRID_STAGE_DRAM_BYTES = 213.85e6 + 5.87e9
 
 
 def parse():
@@ -247,13 +247,16 @@ def run_ours(args, rank, world):
            "visible_paths_per_step": visible_paths, "visible_paths_per_s": visible_paths * world * K / (total_ms / 1e3),
            "rays_per_s": rays * world * K / (total_ms / 1e3), "gpu_launches": launches}
     # roofline of the dominant kernel (scatter->sink grid stage; direct stage for the direct workload)
+    T = int(faces.shape[0])
     if args.workload != "direct":
         s2_ms = sum(a.elapsed_time(b) for a, b in ev["s2_list"]) / K
         tests = int(cnt_s2[1].item()) / K
+        brute_tests = float(Pn) * M * T
         kernel = "grid_stage_kernel (scatter->sink stage incl. its partial-sum reduction)"
     else:
         s2_ms = ms_per_step
         tests = int(cnt_all[1].item()) / K
+        brute_tests = float(N) * M * T
         kernel = "brute_stage_kernel (whole step)"
     achieved = tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12
     peak = fma_rate / 1e12
@@ -261,7 +264,10 @@ def run_ours(args, rank, world):
                        "frac": achieved / peak, "traffic": GRID_STAGE_DRAM_BYTES,
                        "peak_source": "measured FP32 FMA lane-op rate (lyem_fp32_fma_probe, same run; FMA = 1 op)",
                        "tests_per_launch": tests, "ops_per_test": OPS_PER_TEST, "launch_ms": s2_ms,
-                       "share_of_step": s2_ms / ms_per_step}
+                       "share_of_step": s2_ms / ms_per_step,
+                       # the same launch counted in brute-force tests (every ray against every triangle)
+                       "effective_tests_per_s": brute_tests / (s2_ms / 1e3),
+                       "effective_frac": brute_tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12 / peak}
     if clk:
         res["clocks"] = clk
     if rank == 0 and world == 1 and not args.no_sweep:
