@@ -185,14 +185,16 @@ def run_ours(args, rank, world):
             return out.sink
         grid = P.UniformGrid(tris, cell=s.cell)
         o_scat = P.spatial_order(scat)  # scatter points are traced in Morton order
-        out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct).sink
+        o_snk = P.direction_order(snk, grid.centre)  # sinks in direction order from the scene
+        out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct,
+                           snk_order=o_snk).sink
         e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=cnt_all,
                            snk_visible=vis_scat_in, snk_order=o_scat).sink
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
         P.pair_stage(scat, e_p, snk, snk_n, beta=beta, grid=grid, src_W=e_p, sink_out=out, accumulate=True,
-                     counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat)
+                     counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat, snk_order=o_snk)
         b.record()
         if mark:
             ev.setdefault("s2_list", []).append((a, b))

@@ -119,6 +119,17 @@ LYEM_API int lyem_grid_fill(const float *d_tris, int64_t n_tris, const float *or
  * lyem_pair_stage as d_src_order / d_snk_order it makes the rays of a warp
  * coherent.  No counterpart in the reference (it processes pairs in index order). */
 LYEM_API size_t lyem_spatial_order_workspace(int64_t n_points);
+
+/* Direction order of a point set seen from centre3 (host, 3 floats): the
+ * sphere of directions is cut into square (elevation, azimuth) tiles of about
+ * 16 points (edge 4 * sqrt(2 pi^2 / n_points) radians, at least 0.009), tiles
+ * ordered by elevation band then azimuth, so consecutive entries lie in small
+ * angular patches.  Passed as d_snk_order for sinks far from the
+ * scene (far-field spheres) it gives each warp rays of nearly one direction,
+ * hence similar walks; centre3 is typically the centre of the grid box.
+ * Workspace: lyem_spatial_order_workspace(n_points) bytes. */
+LYEM_API int lyem_direction_order(const float *d_points, int64_t n_points, const float *centre3, int32_t *d_order,
+                                  void *d_ws, size_t ws_bytes, void *stream);
 LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t *d_order, void *d_ws,
                                 size_t ws_bytes, void *stream);
 

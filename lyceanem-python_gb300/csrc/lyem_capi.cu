@@ -281,6 +281,19 @@ LYEM_API int lyem_spatial_order(const float* d_points, int64_t n_points, int32_t
     return LYEM_OK;
 }
 
+LYEM_API int lyem_direction_order(const float* d_points, int64_t n_points, const float* centre3, int32_t* d_order,
+                                  void* d_ws, size_t ws_bytes, void* stream) {
+    if (n_points < 0) return LYEM_ERR_INVALID;
+    if (n_points == 0) return LYEM_OK;
+    if (!d_points || !d_order || !centre3) return LYEM_ERR_INVALID;
+    for (int k = 0; k < 3; ++k)
+        if (!isfinite(centre3[k])) return LYEM_ERR_INVALID;
+    if (n_points >= (1LL << 31) - 64) return LYEM_ERR_OVERFLOW;
+    if (!d_ws || ws_bytes < spatial_order_workspace_bytes(n_points)) return LYEM_ERR_WORKSPACE;
+    LYEM_CK(direction_order(d_points, n_points, centre3, d_order, d_ws, as_stream(stream)));
+    return LYEM_OK;
+}
+
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,
                                           int32_t src_chunk) {
     (void)n_tris;

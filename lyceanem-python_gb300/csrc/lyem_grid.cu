@@ -20,6 +20,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "lyem_device.cuh"
 #include "lyem_grid.cuh"
@@ -438,6 +439,58 @@ __global__ void morton_kernel(const float* __restrict__ pts, long long n, const 
         keys[i] = (int)(spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2));
         vals[i] = (int)i;
     }
+}
+
+// Direction tiles: elevation el in [-pi/2, pi/2] and azimuth az in [-pi, pi]
+// of each point seen from c are cut into square tiles of edge `tile` radians
+// (offset by 1/8 tile); the key orders tiles by (elevation band, azimuth
+// tile) and points within a tile by 6-bit (elevation, azimuth) positions.
+// nb * na < 2^18 keeps keys below 2^30.
+__global__ void direction_key_kernel(const float* __restrict__ pts, long long n, float cx, float cy, float cz,
+                                     float tile, int nb, int na, int* keys, int* vals) {
+    const float kPi = 3.14159265358979f;
+    const float inv = 1.f / tile;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float dx = pts[3 * i] - cx, dy = pts[3 * i + 1] - cy, dz = pts[3 * i + 2] - cz;
+        const float fe = (atan2f(dz, hypotf(dx, dy)) + 0.5f * kPi) * inv + 0.125f;
+        const float fa = (atan2f(dy, dx) + kPi) * inv + 0.125f;
+        int key = 0;
+        if (fe == fe && fa == fa) {
+            const float be = fminf(fmaxf(floorf(fe), 0.f), (float)(nb - 1));
+            const float ba = fminf(fmaxf(floorf(fa), 0.f), (float)(na - 1));
+            const int qe = (int)fminf(fmaxf((fe - be) * 64.f, 0.f), 63.f);
+            const int qa = (int)fminf(fmaxf((fa - ba) * 64.f, 0.f), 63.f);
+            key = ((((int)be * na + (int)ba) << 12) | (qe << 6) | qa);
+        }
+        keys[i] = key;
+        vals[i] = (int)i;
+    }
+}
+
+cudaError_t direction_order(const float* pts, long long n, const float* centre3, int* order, void* ws,
+                            cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    int* k0 = static_cast<int*>(ws) + 64;
+    int* v0 = k0 + n + 64;
+    int* k1 = v0 + n + 64;
+    int* v1 = k1 + n + 64;
+    const long long nblocks = (n + kSortTile - 1) / kSortTile;
+    int* hist = v1 + n + 64;
+    int* hist_scanned = hist + 256 * nblocks + 64;
+    int* scan_ws = hist_scanned + 256 * nblocks + 64;
+    long long b = (n + 255) / 256;
+    b = b > 152 * 8 ? 152 * 8 : b;
+    // tiles of about 16 points if the set were an even elevation-azimuth grid (n points over pi x 2 pi)
+    const double kPi = 3.14159265358979323846;
+    const double tile = std::max(0.009, 4.0 * std::sqrt(2.0 * kPi * kPi / (double)n));
+    const int nb = (int)std::ceil(kPi / tile) + 2, na = (int)std::ceil(2.0 * kPi / tile) + 2;
+    direction_key_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, centre3[0], centre3[1], centre3[2], (float)tile,
+                                                          nb, na, k0, v0);
+    note_launches(1);
+    bool first = true;
+    cudaError_t e = radix_sort_pairs(k0, v0, k1, v1, n, 1 << 30, hist, hist_scanned, scan_ws, &first, stream);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(order, first ? v0 : v1, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, stream);
 }
 
 size_t spatial_order_workspace_bytes(long long n) {

@@ -23,6 +23,9 @@ cudaError_t exclusive_scan(const int* in, int* out, long long n, int* ws, cudaSt
 
 size_t spatial_order_workspace_bytes(long long n);
 cudaError_t spatial_order(const float* pts, long long n, int* order, void* ws, cudaStream_t stream);
+// Z-order of the points' directions from centre3 (workspace as spatial_order).
+cudaError_t direction_order(const float* pts, long long n, const float* centre3, int* order, void* ws,
+                            cudaStream_t stream);
 
 size_t grid_count_workspace_bytes(long long n_tris);
 cudaError_t grid_count(const BinSpec& b, const float4* tris, long long n_tris, int* tri_offsets,

@@ -78,6 +78,7 @@ SIGNATURES = {
     "lyem_grid_fill": ([_vp, _i64, _f32p, _f32, _i32p, _vp, _i64, _vp, _vp, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_spatial_order_workspace": ([_i64], _sz),
     "lyem_spatial_order": ([_vp, _i64, _vp, _vp, _sz, _vp], ctypes.c_int),
+    "lyem_direction_order": ([_vp, _i64, _f32p, _vp, _vp, _sz, _vp], ctypes.c_int),
     "lyem_pair_stage_workspace": ([_i64, _i64, _i64, _i32, _i32], _sz),
     "lyem_pair_stage": ([_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _vp, _f32p, _f32, _i32p, _f64, _f64,
                          _i32, _i32, _f32, _vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _sz,

@@ -35,7 +35,8 @@ class SinkField(torch.autograd.Function):
         snk_n = P._points(snk_n)
         E_src = (pol * a.reshape(-1, 1)).contiguous()
         kw = dict(beta=beta, alpha=alpha, grid=grid, tris=tris, self_to_self=self_to_self, want_mask=True)
-        r0 = P.pair_stage(x, E_src, y, snk_n, **kw)
+        o_snk = P.direction_order(y, grid.centre) if grid is not None else None
+        r0 = P.pair_stage(x, E_src, y, snk_n, snk_order=o_snk, **kw)
         E = r0.sink
         have_scat = scat is not None and scat.shape[0] > 0
         if have_scat:
@@ -44,7 +45,8 @@ class SinkField(torch.autograd.Function):
             order = P.spatial_order(scat)
             r1 = P.pair_stage(x, E_src, scat, scat_n, snk_order=order, **kw)
             w = r1.sink
-            r2 = P.pair_stage(scat, w, y, snk_n, src_W=w, sink_out=E, accumulate=True, src_order=order, **kw)
+            r2 = P.pair_stage(scat, w, y, snk_n, src_W=w, sink_out=E, accumulate=True, src_order=order,
+                              snk_order=o_snk, **kw)
             masks = (r0.mask_bits, r1.mask_bits, r2.mask_bits)
         else:
             scat = scat_n = w = None

@@ -134,12 +134,13 @@ class BatchedScattering:
     scenes: sequence of objects with attributes (or dict keys) src [N,3],
       verts [V,3], faces [T,3], optionally E [N,3] complex (default +x),
       scat [P,3] and scat_n [P,3] (scatter points and normals; P may be 0).
-    sinks, sink_normals: [M,3], shared by all scenes.
+    sinks, sink_normals: [M,3], shared by all scenes; processed in direction order seen from their
+      centroid (sink_order="direction", for far-field spheres) or in Morton order ("spatial").
     frequencies (Hz) or betas (rad/m): the frequency list, shared by all scenes.
     Output of run(): complex64 [n_scenes, n_freq, M, 3] on the device."""
 
     def __init__(self, scenes, sinks, sink_normals, frequencies=None, *, betas=None, alpha=0.0, grid_cell=0.5,
-                 self_to_self=False, cull=True, eps=P.EPSILON, config=None, cell_scale=None):
+                 self_to_self=False, cull=True, eps=P.EPSILON, config=None, cell_scale=None, sink_order="direction"):
         if betas is None:
             betas = betas_of(frequencies)
         self.betas = np.ascontiguousarray(np.asarray(betas, np.float64).ravel())
@@ -161,7 +162,10 @@ class BatchedScattering:
                                 get(s, "scat_n"), c) for s, c in zip(scenes, cells)]
         snk = P._points(sinks)
         snk_n = P._points(sink_normals)
-        self.snk_id = P.spatial_order(snk)
+        if sink_order == "direction":  # warps of sinks in one direction from the sinks' centroid
+            self.snk_id = P.direction_order(snk, snk.double().mean(0).tolist())
+        else:
+            self.snk_id = P.spatial_order(snk)
         self.snk = snk.index_select(0, self.snk_id.long()).contiguous()
         self.snk_n = snk_n.index_select(0, self.snk_id.long()).contiguous()
         self.n_scenes, self.n_freq, self.n_snk = len(self.data), self.betas.size, snk.shape[0]

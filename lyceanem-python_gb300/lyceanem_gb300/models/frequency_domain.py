@@ -42,6 +42,12 @@ def _excitation(desired_E_axis, aperture_coords, project_vectors, antenna_axes):
     return (E * area).astype(np.complex64)
 
 
+def _sink_order(dev, snk):
+    """Sinks in direction order seen from the grid's centre (rays of a warp then share a direction and
+    walk similar cells); natural order for brute force."""
+    return P.direction_order(snk, dev.grid.centre) if dev.grid is not None else None
+
+
 def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=None, scattering=0, counters=None,
                cull=True, eps=P.EPSILON):
     """Fused source-summed sink field (complex64 [M,3] CUDA tensor) of the direct path and,
@@ -50,14 +56,17 @@ def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=Non
     kw = dict(tris=dev.tris, grid=dev.grid, alpha=alpha, beta=beta, self_to_self=False, counters=counters, cull=cull,
               eps=eps)
     # Processing order: scatter points (unstructured) are traced in Morton
-    # order; sources and sinks keep the caller's order, which for arrays and
-    # elevation-major far-field grids already puts rays of similar cost in a warp.
-    out = P.pair_stage(src, E, snk, snk_n, **kw).sink
+    # order, sinks in direction order from the scene; sources keep the
+    # caller's order.
+    snk = P._points(snk)
+    o_snk = _sink_order(dev, snk)
+    out = P.pair_stage(src, E, snk, snk_n, snk_order=o_snk, **kw).sink
     if scattering >= 1 and scat is not None and len(scat):
         scat = P._points(scat)
         o_scat = P.spatial_order(scat)
         e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, **kw).sink
-        P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat, **kw)
+        P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat,
+                     snk_order=o_snk, **kw)
     return out
 
 
@@ -127,8 +136,10 @@ def numba_sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat
     kw = dict(tris=dev.tris, grid=dev.grid, alpha=alpha, beta=beta, self_to_self=True, cull=False,
               eps=P.NUMBA_EPSILON)
     snk_n_t = P._points(snk_n)
+    snk = P._points(snk)
+    o_snk = _sink_order(dev, snk)
     if scattering == 0 or los:
-        out = P.pair_stage(src, E, snk, snk_n_t, **kw).sink
+        out = P.pair_stage(src, E, snk, snk_n_t, snk_order=o_snk, **kw).sink
     else:
         out = torch.zeros((snk_n_t.shape[0], 3), dtype=torch.complex64, device=snk_n_t.device)
     if scattering >= 1:
@@ -138,7 +149,7 @@ def numba_sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat
             o = P.spatial_order(scat_t)
             e_p = P.pair_stage(src, E, scat_t, scat_n, snk_order=o, **kw).sink
             tangential_project(e_p, scat_n)
-            P.pair_stage(scat_t, e_p, snk, snk_n_t, sink_out=out, accumulate=True, src_order=o, **kw)
+            P.pair_stage(scat_t, e_p, snk, snk_n_t, sink_out=out, accumulate=True, src_order=o, snk_order=o_snk, **kw)
     return out
 
 

@@ -116,6 +116,11 @@ class UniformGrid:
     def n_cells(self):
         return self.dims[0] * self.dims[1] * self.dims[2]
 
+    @property
+    def centre(self):
+        """Centre of the grid box (the direction origin for far sinks, see direction_order)."""
+        return [self.origin[k] + 0.5 * self.dims[k] * self.cell for k in range(3)]
+
 
 class StageResult:
     __slots__ = ("sink", "pairs", "mask_bits", "counters", "n_src", "n_snk")
@@ -198,6 +203,19 @@ def spatial_order(points):
     if n:
         ws = _ws(lib.lyem_spatial_order_workspace(n), pts.device)
         check(lib.lyem_spatial_order(_p(pts), n, _p(out), _p(ws), ws.numel(), _stream()), "spatial_order")
+    return out
+
+
+def direction_order(points, centre):
+    """Order of a point set by direction seen from `centre` (Z-order of elevation and azimuth; int32
+    permutation on the device).  For far sinks it puts rays of nearly one direction in a warp."""
+    pts = _points(points)
+    n = pts.shape[0]
+    out = torch.empty(n, dtype=torch.int32, device=pts.device)
+    if n:
+        ws = _ws(lib.lyem_spatial_order_workspace(n), pts.device)
+        check(lib.lyem_direction_order(_p(pts), n, f32arr([float(c) for c in centre]), _p(out), _p(ws), ws.numel(),
+                                       _stream()), "direction_order")
     return out
 
 

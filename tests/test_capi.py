@@ -64,3 +64,15 @@ def test_device_entry_points_reject_bad_arguments_without_gpu_work():
     assert lib.lyem_em_bin_counts(None, 0, None, 0, 0, 1, 0.0, 1.0, 0.0, None) == 1
     out = np.zeros(1, np.int32)
     assert lib.lyem_em_bin_counts(None, 0, None, 0, 1, 1, 0.0, -1.0, 0.0, out.ctypes.data) == 1
+
+
+def test_direction_order_argument_checks():
+    """Argument checks of lyem_direction_order run on the host (no device call for these)."""
+    from lyceanem_gb300._native import lib, f32arr
+    c = f32arr([0, 0, 0])
+    assert lib.lyem_direction_order(None, 0, c, None, None, 0, None) == 0  # nothing to order
+    assert lib.lyem_direction_order(None, -1, c, None, None, 0, None) == 1  # LYEM_ERR_INVALID
+    assert lib.lyem_direction_order(None, 5, c, None, None, 0, None) == 1
+    assert lib.lyem_direction_order(ctypes.c_void_p(16), 5, f32arr([0, float("nan"), 0]), ctypes.c_void_p(16),
+                                    None, 0, None) == 1
+    assert lib.lyem_direction_order(ctypes.c_void_p(16), 5, c, ctypes.c_void_p(16), None, 0, None) == 6  # workspace

@@ -355,6 +355,40 @@ def test_spatial_order_and_ordered_stages():
     _no_device_errors()
 
 
+def test_direction_order():
+    """Direction order: a permutation that sorts by (elevation band, azimuth tile, position in the tile)
+    seen from the centre, and ordered stages keep masks and fields."""
+    from lyceanem_gb300 import scenes
+    P = _P()
+    el = np.linspace(-90.0, 90.0, 37)
+    az = np.linspace(-180.0, 180.0, 72, endpoint=False)
+    snk, snk_n, _, _ = scenes.farfield_sinks(10.0, el, az)
+    centre = [0.2, -0.1, 0.05]
+    o = P.direction_order(snk, centre).cpu().numpy()
+    assert sorted(o.tolist()) == list(range(snk.shape[0]))
+    d = snk.astype(np.float64) - np.array(centre)
+    tile = max(0.009, 4 * np.sqrt(2 * np.pi ** 2 / snk.shape[0]))
+    na = int(np.ceil(2 * np.pi / tile)) + 2
+    fe = (np.arctan2(d[:, 2], np.hypot(d[:, 0], d[:, 1])) + np.pi / 2) / tile + 0.125
+    fa = (np.arctan2(d[:, 1], d[:, 0]) + np.pi) / tile + 0.125
+    be, ba = np.floor(fe), np.floor(fa)
+    key = ((be * na + ba).astype(np.int64) << 12) | (np.floor((fe - be) * 64).astype(np.int64) << 6) | \
+        np.floor((fa - ba) * 64).astype(np.int64)
+    # sorted by the key, up to float32-vs-float64 rounding of points on a quantisation boundary
+    assert np.mean(np.diff(key[o]) < 0) < 0.01
+    src, _, _, v, f, _ = random_scene(32, n_src=40, n_snk=10, n_tris=400)
+    E = np.tile(np.array([[1, 0, 0]], np.complex64), (40, 1))
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    g = P.UniformGrid(tris, cell=0.3)
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f))
+    a = P.pair_stage(src, E, snk, snk_n, beta=80.0, grid=g, want_mask=True)
+    b = P.pair_stage(src, E, snk, snk_n, beta=80.0, grid=g, want_mask=True,
+                     snk_order=P.direction_order(snk, g.centre))
+    assert np.array_equal(b.mask().cpu().numpy(), om)
+    assert torch.equal(a.sink, b.sink)  # one writer per sink, same chunk order
+    _no_device_errors()
+
+
 @pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3", 1e-4), ("fp16x3", 1e-5)])
 def test_beam_sweep_modes_against_fp64(mode, tol):
     """Beam sweep of a formed network against a complex128 product of the same network."""
