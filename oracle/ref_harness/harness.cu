@@ -13,6 +13,11 @@
 // thread rewrites without a barrier (raycasting_brute_force.cuh:36-43).
 #include "raycasting.cuh"
 #include "em.cuh"
+// Also puts the reference's own set_values and raycast_brute_force kernels
+// (lyceanem/src/raycasting.cuh:97-108, raycasting_brute_force.cuh:68-88) into
+// the cubin, so that time_ref.py can launch them as raycast_wrapper_brute_force
+// does (<<<32, 512>>>, raycasting_brute_force.cuh:152-170) and time them.
+#include "raycasting_brute_force.cuh"
 
 extern "C" __global__ void ref_pairs(float3* source, float3* end, float4* ray, int source_num, int end_num, int flag,
                                      float3* tri_vertex, int3* triangle_index, int tri_num, PointData* points,
