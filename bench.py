@@ -385,7 +385,7 @@ def run_sweep(args, n_check=256, reps=5):
 
 
 # ------------------------------------------------------------------ batched
-BATCH_TUNE_CANDIDATES = [(2, 64, 8), (1, 64, 8), (4, 64, 8)]
+BATCH_TUNE_CANDIDATES = [(2, 64, 8), (2, 64, 6), (1, 64, 8), (4, 64, 8)]
 # grid cell edge per scene = k * (box volume / triangles)^(1/3); the autotuner picks k
 BATCH_TUNE_CELL_SCALES = [1.0, 1.25, 1.5]
 

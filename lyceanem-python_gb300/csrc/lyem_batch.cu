@@ -646,14 +646,15 @@ cudaError_t launch_batch_t(const BatchParams& P, int blocks_per_sm, cudaStream_t
 template <bool CULL>
 cudaError_t launch_batch_c(const BatchParams& P, int fg, int bps, cudaStream_t s, int* b) {
     // register-capped variants: 8 (32 registers) or 4 blocks per SM for up
-    // to 4 frequencies per thread, 3 for 4 and 8; other requests run the
-    // uncapped variant
+    // to 4 frequencies per thread, also 6 (40 registers) for 2, 3 for 4 and 8;
+    // other requests run the uncapped variant
     switch (fg) {
         case 1:
             if (bps == 8) return launch_batch_t<CULL, 1, 8>(P, bps, s, b);
             return bps == 4 ? launch_batch_t<CULL, 1, 4>(P, bps, s, b) : launch_batch_t<CULL, 1, 1>(P, bps, s, b);
         case 2:
             if (bps == 8) return launch_batch_t<CULL, 2, 8>(P, bps, s, b);
+            if (bps == 6) return launch_batch_t<CULL, 2, 6>(P, bps, s, b);
             return bps == 4 ? launch_batch_t<CULL, 2, 4>(P, bps, s, b) : launch_batch_t<CULL, 2, 1>(P, bps, s, b);
         case 4:
             if (bps == 8) return launch_batch_t<CULL, 4, 8>(P, bps, s, b);

@@ -33,13 +33,14 @@ from ._native import BatchConfig, BatchScene, LyemError, check, lib
 C0 = 299792458.0
 
 # (frequencies per thread, sources per visibility item, blocks per SM).  Blocks per
-# SM 3, 4 or 8 select kernel variants whose registers are capped for that
+# SM 3, 4, 6 or 8 select kernel variants whose registers are capped for that
 # occupancy; 0 runs the uncapped variant with as many blocks as fit.  On the
-# 64-scene batch (4.0e9 ray pairs, 9.9e11 ray-triangle tests) one launch took
+# 64-scene batch with one 0.5 m cell (4.0e9 ray pairs, 9.9e11 ray-triangle tests) one launch took
 # 5.41 s at (4, 64, 4) and 4.49 / 5.36 / 4.71 s at (2 / 1 / 4, 64, 8): the
 # visibility phase dominates and gains from the extra resident warps more
 # than the field phase loses to spilling.
-CANDIDATES = [(2, 64, 8), (1, 64, 8), (4, 64, 8), (2, 32, 8), (4, 64, 4), (4, 32, 3), (8, 32, 3), (4, 32, 0)]
+CANDIDATES = [(2, 64, 8), (2, 64, 6), (1, 64, 8), (4, 64, 8), (2, 32, 8), (4, 64, 4), (4, 32, 3), (8, 32, 3),
+              (4, 32, 0)]
 DEFAULT = (2, 64, 8)
 
 
