@@ -278,10 +278,9 @@ def test_edge_sizes(n_src, n_snk, n_tris):
     r = P.pair_stage(src, E, snk, snk_n, beta=beta, tris=tris, want_mask=True, want_pairs=True)
     assert np.array_equal(r.mask().cpu().numpy(), om)
     assert rel_err(r.sink.cpu().numpy(), ref) < FIELD_TOL
-    if n_tris:
-        g = P.UniformGrid(tris)
-        r = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=g, want_mask=True)
-        assert np.array_equal(r.mask().cpu().numpy(), om)
+    g = P.UniformGrid(tris)  # also with no triangles: a one-cell grid whose cell table is empty
+    r = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=g, want_mask=True)
+    assert np.array_equal(r.mask().cpu().numpy(), om)
     _no_device_errors()
 
 
