@@ -352,7 +352,7 @@ def run_sweep(args, n_check=256, reps=5):
     res = {"n_elements": N, "n_sinks": M, "n_beams": K, "network_form_ms": form_ms,
            "algorithmic_flops": flops}
     outs = {}
-    for mode in ("fp32", "bf16x3", "fp16x3"):
+    for mode in ("fp32", "bf16x3", "fp16x3", "bf16x3g", "fp16x3g"):
         sw = BS.BeamSweep(G, mode)
         out = sw.run(W)
         torch.cuda.synchronize()
@@ -380,6 +380,8 @@ def run_sweep(args, n_check=256, reps=5):
         res[mode]["rel_err_fp64"] = float(np.linalg.norm(E - E64) / np.linalg.norm(E64))
     res["speedup_bf16x3_vs_fp32"] = res["fp32"]["ms"] / res["bf16x3"]["ms"]
     res["speedup_fp16x3_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3"]["ms"]
+    res["speedup_bf16x3g_vs_fp32"] = res["fp32"]["ms"] / res["bf16x3g"]["ms"]
+    res["speedup_fp16x3g_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3g"]["ms"]
     res["error_sample"] = f"{n_check} seeded sinks x {K} beams x 3 components, relative Frobenius norm"
     return res
 

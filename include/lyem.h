@@ -233,6 +233,14 @@ LYEM_API int lyem_sweep_prepare_weights(const float *d_W, int64_t n_src, int64_t
                                         void *stream);
 LYEM_API int lyem_sweep_run(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
                             const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *stream);
+/* Modes 3 (BF16) and 4 (FP16): the same split with the complex product in three
+ * real products (Gauss: Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi)), 6 M N K flops per
+ * component instead of 8; they need a scratch of lyem_sweep_workspace_bytes
+ * (three FP32 ld x n_beams products) and lyem_sweep_run_ws (any mode). */
+LYEM_API size_t lyem_sweep_workspace_bytes(int64_t ld, int64_t n_beams, int32_t mode);
+LYEM_API int lyem_sweep_run_ws(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
+                               const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *d_ws,
+                               size_t ws_bytes, void *stream);
 
 /* --------------------------------------------------------------- adjoint */
 

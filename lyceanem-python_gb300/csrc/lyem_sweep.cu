@@ -14,7 +14,15 @@
 //      product is hi*hi + hi*lo + lo*hi on the tensor cores with FP32
 //      accumulation (lo*lo, ~2^-16 relative, is dropped);
 //   2  FP16 split, same scheme with binary16 (11 + 11 significant bits).
-// For the split modes the complex product is one real GEMM in interleaved form:
+//   3, 4  BF16 / FP16 split with the complex product in three real products
+//      (Gauss): with G = Gr + j Gi and W = Wr + j Wi,
+//        T1 = Gr Wr,  T2 = Gi Wi,  T3 = (Gr + Gi)(Wr + Wi),
+//        Re E = T1 - T2,  Im E = T3 - T1 - T2,
+//      each T a real (M x N)(N x K) GEMM of split operands (6 M N K flops per
+//      component against 8 M N K), the sums Gr + Gi and Wr + Wi formed in FP32
+//      before the split.  The three split products of one T run as two GEMMs:
+//      [hi | lo] (M x 2N) times [hi ; hi] (2N x K), then hi times lo.
+// For the split modes 1, 2 the complex product is one real GEMM in interleaved form:
 //   A' = [G | jG] as a (2M x 2N) real column-major matrix (column n holds the
 //   interleaved (re, im) of G[:, n]; column N + n holds j G[:, n] = (-im, re)),
 //   B' = [Re W^T ; Im W^T] (2N x K),
@@ -75,6 +83,66 @@ __global__ void split_network_kernel(const float2* __restrict__ pairs, long long
             lp[colj + 2 * m] = to_lp<T>(-from_lp<T>(li));
             lp[colj + 2 * m + 1] = lr;
         }
+    }
+}
+
+// Network [N][M][3] -> per component six planes (ld x N, column-major, rows
+// past M zero): Gr hi, Gr lo, Gi hi, Gi lo, Gs hi, Gs lo (Gs = Gr + Gi), so that
+// each part's hi and lo planes form one (ld x 2N) matrix.
+template <typename T>
+__global__ void split_network_gauss_kernel(const float2* __restrict__ pairs, long long N, long long M, long long ld,
+                                           T* __restrict__ out) {
+    const long long plane = ld * N;
+    const long long total = N * ld;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long n = i / ld, m = i - n * ld;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 g = m < M ? pairs[(n * M + m) * 3 + c] : make_float2(0.f, 0.f);
+            const float part[3] = {g.x, g.y, __fadd_rn(g.x, g.y)};
+            T* base = out + (long long)(6 * c) * plane;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const T h = to_lp<T>(part[q]);
+                base[(2 * q) * plane + i] = h;
+                base[(2 * q + 1) * plane + i] = to_lp<T>(part[q] - from_lp<T>(h));
+            }
+        }
+    }
+}
+
+// Weights W [K][N] -> per part (r, i, s = r + i) a (2N x K) column-major
+// [hi ; hi] matrix followed by a (N x K) lo matrix.
+template <typename T>
+__global__ void split_weights_gauss_kernel(const float2* __restrict__ W, long long N, long long K, T* __restrict__ out) {
+    const long long part_elems = 3 * N * K;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N * K;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long k = i / N, n = i - k * N;
+        const float2 w = W[i];
+        const float part[3] = {w.x, w.y, __fadd_rn(w.x, w.y)};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            T* dup = out + q * part_elems;
+            T* lo = dup + 2 * N * K;
+            const T h = to_lp<T>(part[q]);
+            dup[k * 2 * N + n] = h;
+            dup[k * 2 * N + N + n] = h;
+            lo[k * N + n] = to_lp<T>(part[q] - from_lp<T>(h));
+        }
+    }
+}
+
+// out (complex64, column-major ld x K with leading dimension ldc) from the three
+// real products T1, T2, T3 (ld x K each, consecutive in t).
+__global__ void gauss_combine_kernel(const float* __restrict__ t, long long ld, long long K, long long ldc,
+                                     float2* __restrict__ out) {
+    const long long n = ld * K;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float t1 = t[i], t2 = t[n + i], t3 = t[2 * n + i];
+        const long long k = i / ld, m = i - k * ld;
+        out[k * ldc + m] = make_float2(__fsub_rn(t1, t2), __fsub_rn(__fsub_rn(t3, t1), t2));
     }
 }
 
@@ -143,17 +211,24 @@ extern "C" {
 LYEM_API size_t lyem_sweep_network_bytes(int64_t n_src, int64_t ld, int32_t mode) {
     if (n_src <= 0 || ld <= 0) return 0;
     if (mode == 0) return (size_t)3 * n_src * ld * 8;
+    if (mode >= 3) return (size_t)3 * 6 * ld * n_src * 2;
     return (size_t)3 * 2 * (2 * ld) * (2 * n_src) * 2;
 }
 
 LYEM_API size_t lyem_sweep_weights_bytes(int64_t n_src, int64_t n_beams, int32_t mode) {
     if (n_src <= 0 || n_beams <= 0 || mode == 0) return 0;
+    if (mode >= 3) return (size_t)3 * 3 * n_src * n_beams * 2;
     return (size_t)2 * (2 * n_src) * n_beams * 2;
+}
+
+LYEM_API size_t lyem_sweep_workspace_bytes(int64_t ld, int64_t n_beams, int32_t mode) {
+    if (ld <= 0 || n_beams <= 0 || mode < 3) return 0;
+    return (size_t)3 * ld * n_beams * 4;
 }
 
 LYEM_API int lyem_sweep_prepare_network(const float* d_pairs, int64_t n_src, int64_t n_snk, int32_t mode, int64_t ld,
                                         void* d_network, void* stream) {
-    if (n_src < 0 || n_snk < 0 || mode < 0 || mode > 2 || ld < n_snk || (ld & 7)) return LYEM_ERR_INVALID;
+    if (n_src < 0 || n_snk < 0 || mode < 0 || mode > 4 || ld < n_snk || (ld & 7)) return LYEM_ERR_INVALID;
     if (n_src == 0 || n_snk == 0) return LYEM_OK;
     if (!d_pairs || !d_network) return LYEM_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -164,6 +239,11 @@ LYEM_API int lyem_sweep_prepare_network(const float* d_pairs, int64_t n_src, int
     else if (mode == 1)
         split_network_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, 1.f,
                                                              reinterpret_cast<__nv_bfloat16*>(d_network));
+    else if (mode == 3)
+        split_network_gauss_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(P, n_src, n_snk, ld,
+                                                                   reinterpret_cast<__nv_bfloat16*>(d_network));
+    else if (mode == 4)
+        split_network_gauss_kernel<__half><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, reinterpret_cast<__half*>(d_network));
     else
         split_network_kernel<__half><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, 1.f, reinterpret_cast<__half*>(d_network));
     note_launches(1);
@@ -172,7 +252,7 @@ LYEM_API int lyem_sweep_prepare_network(const float* d_pairs, int64_t n_src, int
 
 LYEM_API int lyem_sweep_prepare_weights(const float* d_W, int64_t n_src, int64_t n_beams, int32_t mode, void* d_B,
                                         void* stream) {
-    if (n_src < 0 || n_beams < 0 || mode < 0 || mode > 2) return LYEM_ERR_INVALID;
+    if (n_src < 0 || n_beams < 0 || mode < 0 || mode > 4) return LYEM_ERR_INVALID;
     if (mode == 0 || n_src == 0 || n_beams == 0) return LYEM_OK;
     if (!d_W || !d_B) return LYEM_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -180,16 +260,33 @@ LYEM_API int lyem_sweep_prepare_weights(const float* d_W, int64_t n_src, int64_t
     const unsigned b = sweep_blocks(n_src * n_beams);
     if (mode == 1)
         split_weights_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__nv_bfloat16*>(d_B));
-    else
+    else if (mode == 2)
         split_weights_kernel<__half><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__half*>(d_B));
+    else if (mode == 3)
+        split_weights_gauss_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(W, n_src, n_beams,
+                                                                   reinterpret_cast<__nv_bfloat16*>(d_B));
+    else
+        split_weights_gauss_kernel<__half><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__half*>(d_B));
     note_launches(1);
     return cudaGetLastError() == cudaSuccess ? LYEM_OK : LYEM_ERR_CUDA;
 }
 
+LYEM_API int lyem_sweep_run_ws(const void* d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float* d_W,
+                               const void* d_B, int64_t n_beams, int32_t mode, float* d_out, int64_t ldc, void* d_ws,
+                               size_t ws_bytes, void* stream);
+
 LYEM_API int lyem_sweep_run(const void* d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float* d_W,
                             const void* d_B, int64_t n_beams, int32_t mode, float* d_out, int64_t ldc, void* stream) {
-    if (n_src <= 0 || n_snk <= 0 || n_beams <= 0 || mode < 0 || mode > 2 || ld < n_snk || ldc < ld)
+    if (mode > 2) return LYEM_ERR_INVALID;  // the three-product modes need lyem_sweep_run_ws
+    return lyem_sweep_run_ws(d_network, n_src, n_snk, ld, d_W, d_B, n_beams, mode, d_out, ldc, nullptr, 0, stream);
+}
+
+LYEM_API int lyem_sweep_run_ws(const void* d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float* d_W,
+                               const void* d_B, int64_t n_beams, int32_t mode, float* d_out, int64_t ldc, void* d_ws,
+                               size_t ws_bytes, void* stream) {
+    if (n_src <= 0 || n_snk <= 0 || n_beams <= 0 || mode < 0 || mode > 4 || ld < n_snk || ldc < ld)
         return LYEM_ERR_INVALID;
+    if (mode >= 3 && (!d_ws || ws_bytes < lyem_sweep_workspace_bytes(ld, n_beams, mode))) return LYEM_ERR_WORKSPACE;
     if (!d_network || !d_out || (mode == 0 && !d_W) || (mode != 0 && !d_B)) return LYEM_ERR_INVALID;
     if (n_src > 0x7fffffffLL / 2 || 2 * ld > 0x7fffffffLL || n_beams > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -198,8 +295,34 @@ LYEM_API int lyem_sweep_run(const void* d_network, int64_t n_src, int64_t n_snk,
     cublasHandle_t h = cublas_for_current_device(s, &err);
     if (err) return LYEM_ERR_CUDA;
     for (int c = 0; c < 3; ++c) {
-        cublasStatus_t st;
-        if (mode == 0) {
+        cublasStatus_t st = CUBLAS_STATUS_SUCCESS;
+        if (mode >= 3) {
+            const cudaDataType_t dt = mode == 3 ? CUDA_R_16BF : CUDA_R_16F;
+            const size_t plane = (size_t)ld * n_src;
+            const size_t part_b = (size_t)3 * n_src * n_beams;
+            float* T = static_cast<float*>(d_ws);
+            const float one = 1.f, zero = 0.f;
+            const int m = (int)ld, n = (int)n_beams, k = (int)n_src;
+            for (int q = 0; q < 3 && st == CUBLAS_STATUS_SUCCESS; ++q) {
+                const unsigned short* Ahi = reinterpret_cast<const unsigned short*>(d_network) + (6 * c + 2 * q) * plane;
+                const unsigned short* Bdup = reinterpret_cast<const unsigned short*>(d_B) + q * part_b;
+                const unsigned short* Blo = Bdup + (size_t)2 * n_src * n_beams;
+                float* C = T + (size_t)q * ld * n_beams;
+                // [hi | lo] x [hi ; hi] = hi*hi + lo*hi, then += hi*lo
+                st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, 2 * k, &one, Ahi, dt, m, Bdup, dt, 2 * k, &zero,
+                                  C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+                if (st == CUBLAS_STATUS_SUCCESS)
+                    st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, Ahi, dt, m, Blo, dt, k, &one, C,
+                                      CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+                note_launches(2);
+            }
+            if (st == CUBLAS_STATUS_SUCCESS) {
+                gauss_combine_kernel<<<sweep_blocks(ld * n_beams), 256, 0, s>>>(
+                    T, ld, n_beams, ldc, reinterpret_cast<float2*>(d_out) + (size_t)c * n_beams * ldc);
+                note_launches(1);
+                if (cudaGetLastError() != cudaSuccess) return LYEM_ERR_CUDA;
+            }
+        } else if (mode == 0) {
             const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
             const cuComplex* A = reinterpret_cast<const cuComplex*>(d_network) + (size_t)c * n_src * ld;
             // the operand rows past n_snk are zero padding: run the aligned row count

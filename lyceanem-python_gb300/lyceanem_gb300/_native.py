@@ -96,6 +96,8 @@ SIGNATURES = {
     "lyem_sweep_weights_bytes": ([_i64, _i64, _i32], _sz),
     "lyem_sweep_prepare_network": ([_vp, _i64, _i64, _i32, _i64, _vp, _vp], ctypes.c_int),
     "lyem_sweep_prepare_weights": ([_vp, _i64, _i64, _i32, _vp, _vp], ctypes.c_int),
+    "lyem_sweep_workspace_bytes": ([_i64, _i64, _i32], _sz),
+    "lyem_sweep_run_ws": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp, _sz, _vp], ctypes.c_int),
     "lyem_sweep_run": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_batch_workspace": ([_scp, _i32, _i64, _i32, _cfgp], _sz),
     "lyem_batch_items": ([_scp, _i32, _i64, _i32, _cfgp, _i64p], ctypes.c_int64),

@@ -6,7 +6,9 @@ scene is formed once on the device (pair stage with unit excitations) and the
 sink fields of K excitation vectors are three complex GEMMs:
     E[m, k, c] = sum_n G[n, m, c] W[k, n].
 Modes: "fp32" (cublasCgemm), "bf16x3" and "fp16x3" (hi/lo split, three products
-on the tensor cores with FP32 accumulation).
+on the tensor cores with FP32 accumulation), "bf16x3g" and "fp16x3g" (the same
+split with each complex product formed from three real products, Gauss's
+Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi): 6 instead of 8 M N K flops per component).
 """
 import ctypes
 
@@ -15,7 +17,7 @@ import torch
 from . import propagation as P
 from ._native import check, lib
 
-MODES = {"fp32": 0, "bf16x3": 1, "fp16x3": 2}
+MODES = {"fp32": 0, "bf16x3": 1, "fp16x3": 2, "bf16x3g": 3, "fp16x3g": 4}
 
 
 def _p(t):
@@ -48,6 +50,7 @@ class BeamSweep:
         check(lib.lyem_sweep_prepare_network(_p(torch.view_as_real(net)), self.n_src, self.n_snk, self.mode, self.ld,
                                              _p(self.operand), P._stream()), "sweep_prepare_network")
         self._wbuf = None
+        self._ws = None
 
     def run(self, W, out=None):
         """Sink fields for excitations W complex [K, N]: returns complex64 [3, K, ld] (use .fields())."""
@@ -63,8 +66,13 @@ class BeamSweep:
                                                  P._stream()), "sweep_prepare_weights")
         if out is None:
             out = torch.empty((3, K, self.ld), dtype=torch.complex64, device=W.device)
-        check(lib.lyem_sweep_run(_p(self.operand), self.n_src, self.n_snk, self.ld, _p(torch.view_as_real(W)), _p(B),
-                                 K, self.mode, _p(torch.view_as_real(out)), self.ld, P._stream()), "sweep_run")
+        nws = lib.lyem_sweep_workspace_bytes(self.ld, K, self.mode)
+        if nws and (self._ws is None or self._ws.numel() < nws):
+            self._ws = torch.empty(nws, dtype=torch.uint8, device=W.device)
+        ws = self._ws if nws else None
+        check(lib.lyem_sweep_run_ws(_p(self.operand), self.n_src, self.n_snk, self.ld, _p(torch.view_as_real(W)),
+                                    _p(B), K, self.mode, _p(torch.view_as_real(out)), self.ld, _p(ws),
+                                    0 if ws is None else ws.numel(), P._stream()), "sweep_run")
         return out
 
     def fields(self, out):

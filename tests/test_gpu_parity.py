@@ -388,7 +388,8 @@ def test_direction_order():
     _no_device_errors()
 
 
-@pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3", 1e-4), ("fp16x3", 1e-5)])
+@pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3", 1e-4), ("fp16x3", 1e-5), ("bf16x3g", 1e-4),
+                                      ("fp16x3g", 2e-5)])
 def test_beam_sweep_modes_against_fp64(mode, tol):
     """Beam sweep of a formed network against a complex128 product of the same network."""
     from lyceanem_gb300 import beam_sweep as BS
