@@ -345,13 +345,27 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == k
     unsigned long long blocked = 0, tests = 0;
     Walk w;
     if (MODE != kRefill) {
+        // per source of the chunk, the triangle nearest to it (one warp per source):
+        // tried first by every ray from that source
+        __shared__ int s_hint[kGridMaxChunk];
+        for (int s = tid >> 5; s < nsrc; s += kThreads / 32) {
+            const float* so = p.src_pos + 3 * src_index(s);
+            const int h = warp_nearest_ref(p, so[0], so[1], so[2]);
+            if ((tid & 31) == 0) s_hint[s] = h;
+        }
+        __syncthreads();
         for (int s = 0; s < nsrc; ++s) {
             const long long n = src_index(s);
             if (!m_ok || (p.skip_diag && n == m)) continue;
             const float* so = p.src_pos + 3 * n;
             if (!walk_begin(p, w, so[0], so[1], so[2], ex, ey, ez)) continue;
+            const int hint = s_hint[s];
             bool hit = false;
-            while (true) {
+            if (hint >= 0) {
+                ++tests;
+                hit = walk_test_ref<CULL>(p, w, hint);
+            }
+            while (!hit) {
                 while (w.q < w.q1) {
                     ++tests;
                     if (walk_test<CULL>(p, w)) { hit = true; break; }

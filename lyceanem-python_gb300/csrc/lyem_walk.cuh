@@ -91,6 +91,61 @@ __device__ __forceinline__ bool walk_test(const GP& p, Walk& w) {
     return hit_full<CULL>(w.r, w.ox, w.oy, w.oz, v0, e1, e2, p.eps);
 }
 
+// Cell-order reference of the triangle of o's cell whose centroid is nearest
+// to point o relative to the triangle's size (squared distance over squared
+// longest edge), if o lies within that size of it; -1 otherwise (o off every
+// triangle of its cell, outside the grid box, or its cell empty).  Called by
+// all 32 lanes of a warp with the same o; every lane gets the same answer.  A
+// ray leaving a point that lies on (or just off) a surface is most often
+// blocked by that surface's own triangle, so the walk tries this one first.
+template <class GP>
+__device__ __forceinline__ int warp_nearest_ref(const GP& p, float ox, float oy, float oz) {
+    int q0 = 0, q1 = 0;
+    const float fx = (ox - p.g0[0]) * p.inv_cell, fy = (oy - p.g0[1]) * p.inv_cell, fz = (oz - p.g0[2]) * p.inv_cell;
+    if (fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)p.dims[0] && fy < (float)p.dims[1] &&
+        fz < (float)p.dims[2]) {
+        const int c = ((int)fz * p.dims[1] + (int)fy) * p.dims[0] + (int)fx;
+        q0 = __float_as_int(__ldg(&p.cell_box[2 * (long long)c].w));
+        q1 = __float_as_int(__ldg(&p.cell_box[2 * (long long)c + 1].w));
+    }
+    const int lane = threadIdx.x & 31;
+    float best = __int_as_float(0x7f800000);
+    int ref = -1;
+    for (int r = q0 + lane; r < q1; r += 32) {
+        const float4* t = p.cell_tris + 3 * (long long)r;
+        const float4 v0 = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
+        const float cx = v0.x + (e1.x + e2.x) * (1.f / 3.f) - ox;
+        const float cy = v0.y + (e1.y + e2.y) * (1.f / 3.f) - oy;
+        const float cz = v0.z + (e1.z + e2.z) * (1.f / 3.f) - oz;
+        const float fx = e2.x - e1.x, fy = e2.y - e1.y, fz = e2.z - e1.z;
+        const float l2 = fmaxf(fmaxf(e1.x * e1.x + e1.y * e1.y + e1.z * e1.z, e2.x * e2.x + e2.y * e2.y + e2.z * e2.z),
+                               fx * fx + fy * fy + fz * fz);
+        const float d2 = cx * cx + cy * cy + cz * cz;
+        if (d2 < l2 && d2 < best * l2) {  // d2 / l2 < best, without a division
+            best = d2 / l2;
+            ref = r;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float b2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int r2 = __shfl_xor_sync(0xffffffffu, ref, o);
+        if (b2 < best || (b2 == best && r2 > ref)) {  // ties: any fixed rule, the same in every lane
+            best = b2;
+            ref = r2;
+        }
+    }
+    return ref;
+}
+
+// Tests the walk's segment against cell-order reference q (any triangle of the
+// scene: a hit there blocks the segment just as one found by the walk).
+template <bool CULL, class GP>
+__device__ __forceinline__ bool walk_test_ref(const GP& p, const Walk& w, int q) {
+    const float4* t = p.cell_tris + 3 * (long long)q;
+    return hit_full<CULL>(w.r, w.ox, w.oy, w.oz, __ldg(t), __ldg(t + 1), __ldg(t + 2), p.eps);
+}
+
 // Crosses the nearest cell boundary; false when the segment or the grid ends there.
 template <class GP>
 __device__ __forceinline__ bool walk_step(const GP& p, Walk& w, unsigned int* err) {
