@@ -358,13 +358,14 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == k
             const long long n = src_index(s);
             if (!m_ok || (p.skip_diag && n == m)) continue;
             const float* so = p.src_pos + 3 * n;
-            if (!walk_begin(p, w, so[0], so[1], so[2], ex, ey, ez)) continue;
+            walk_ray(w, so[0], so[1], so[2], ex, ey, ez);
             const int hint = s_hint[s];
             bool hit = false;
-            if (hint >= 0) {
+            if (hint >= 0) {  // a hit on any triangle blocks the segment, walked or not
                 ++tests;
                 hit = walk_test_ref<CULL>(p, w, hint);
             }
+            if (!hit && !walk_setup(p, w)) continue;
             while (!hit) {
                 while (w.q < w.q1) {
                     ++tests;

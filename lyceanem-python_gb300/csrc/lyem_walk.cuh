@@ -50,12 +50,16 @@ __device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
     if (out || __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax) w.q = w.q1;
 }
 
-// Starts the walk of segment o -> e; false if the segment misses the grid box.
-template <class GP>
-__device__ __forceinline__ bool walk_begin(const GP& p, Walk& w, float ox, float oy, float oz, float ex,
-                                           float ey, float ez) {
+// The segment o -> e of a walk (origin and ray); enough for walk_test_ref.
+__device__ __forceinline__ void walk_ray(Walk& w, float ox, float oy, float oz, float ex, float ey, float ez) {
     w.ox = ox; w.oy = oy; w.oz = oz;
     w.r = make_ray(ox, oy, oz, ex, ey, ez);
+}
+
+// Enters the grid along the segment set by walk_ray; false if it misses the grid box.
+template <class GP>
+__device__ __forceinline__ bool walk_setup(const GP& p, Walk& w) {
+    const float ox = w.ox, oy = w.oy, oz = w.oz;
     float t0 = 0.f;
     w.t1 = w.r.len;
     bool miss = false;
@@ -80,6 +84,14 @@ __device__ __forceinline__ bool walk_begin(const GP& p, Walk& w, float ox, float
     w.guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
     walk_enter(p, w, (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx);
     return true;
+}
+
+// Starts the walk of segment o -> e; false if the segment misses the grid box.
+template <class GP>
+__device__ __forceinline__ bool walk_begin(const GP& p, Walk& w, float ox, float oy, float oz, float ex,
+                                           float ey, float ez) {
+    walk_ray(w, ox, oy, oz, ex, ey, ez);
+    return walk_setup(p, w);
 }
 
 // Tests triangle q of the current cell and advances q; true on a hit.
