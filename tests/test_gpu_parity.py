@@ -125,6 +125,48 @@ def test_grazing_rays_masks_bit_exact(eps):
     _no_device_errors()
 
 
+@pytest.mark.parametrize("cull", [True, False])
+def test_lattice_scene_masks_bit_exact(cull):
+    """Axis-aligned geometry on a lattice: axis-aligned quads lying on cell faces, sources and sinks on cell
+    planes, rays along the axes (zero direction components) and at 45 degrees; the grid walk (cell boxes,
+    own-surface hint, direction order) against the oracle's brute force, both visibility rules."""
+    P = _P()
+    cell = 0.25
+    quads = []
+    for k in range(-3, 4):          # planes z = k * cell, x = k * cell (exactly on cell faces)
+        for a in range(-2, 2):
+            for b in range(-2, 2):
+                u0, u1, v0, v1 = a * cell, (a + 1) * cell, b * cell, (b + 1) * cell
+                if (a + b + k) % 2 == 0:
+                    quads.append([[u0, v0, k * cell], [u1, v0, k * cell], [u1, v1, k * cell], [u0, v1, k * cell]])
+                else:
+                    quads.append([[k * cell, u0, v0], [k * cell, u1, v0], [k * cell, u1, v1], [k * cell, u0, v1]])
+    q = np.array(quads, np.float32)
+    v = q.reshape(-1, 3)
+    f = np.concatenate([np.stack([4 * i + np.array([0, 1, 2]), 4 * i + np.array([0, 2, 3])]) for i in range(len(q))])
+    f = f.astype(np.int32)
+    g1 = np.arange(-4, 5) * cell
+    src = np.array([[x, y, z] for x in g1[::2] for y in g1[::3] for z in (-1.0, 0.5 * cell, 1.0)], np.float32)
+    snk = np.concatenate([
+        np.array([[x, y, 2.0] for x in g1 for y in g1], np.float32),           # straight up from lattice points
+        np.array([[2.0, y, z] for y in g1[::2] for z in g1[::2]], np.float32),  # along +x
+        np.array([[x, x, -2.0] for x in g1], np.float32),                       # 45 degree diagonals
+    ])
+    snk_n = -snk / np.linalg.norm(snk, axis=1, keepdims=True)
+    eps = 1e-6 if cull else 1e-7
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f), cull=cull, eps=eps)
+    assert 0 < om.sum() < om.size
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    E = np.tile(np.array([[1, 0, 0]], np.complex64), (src.shape[0], 1))
+    for c in (cell, 2 * cell, None):
+        g = P.UniformGrid(tris, cell=c)
+        for order in (None, P.direction_order(snk, g.centre)):
+            r = P.pair_stage(src, E, snk, snk_n, beta=20.0, grid=g, cull=cull, eps=eps, want_mask=True,
+                             snk_order=order)
+            assert np.array_equal(r.mask().cpu().numpy(), om), (c, order is None)
+    _no_device_errors()
+
+
 def test_grid_build_matches_cpu_binning():
     """Cell ranges of the device grid equal a NumPy restatement of the padded-box binning."""
     P = _P()
