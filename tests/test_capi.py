@@ -76,3 +76,33 @@ def test_direction_order_argument_checks():
     assert lib.lyem_direction_order(ctypes.c_void_p(16), 5, f32arr([0, float("nan"), 0]), ctypes.c_void_p(16),
                                     None, 0, None) == 1
     assert lib.lyem_direction_order(ctypes.c_void_p(16), 5, c, ctypes.c_void_p(16), None, 0, None) == 6  # workspace
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """include/lyem.h is plain C: a C program that includes it links against liblyem_gpu.so and calls the
+    host-only entry points (no GPU needed)."""
+    import os
+    import shutil
+    import subprocess
+    from lyceanem_gb300 import _native
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "lyem.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "  float org[3], cell; int32_t dims[3];\n"
+        "  const float b[6] = {-10.f, -10.f, -1.f, 10.f, 10.f, 5.f};\n"
+        "  if (lyem_grid_plan(b, 120000, 0.5f, org, &cell, dims) != LYEM_OK) return 1;\n"
+        '  printf("%d %s %d %d %d\\n", lyem_version(), lyem_status_string(LYEM_ERR_WORKSPACE), dims[0], dims[1],\n'
+        "         dims[2]);\n"
+        "  return 0;\n}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_native.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(root, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-llyem_gpu", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(out[0]) >= 100 and out[-3:] == ["41", "41", "13"]
