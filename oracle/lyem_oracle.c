@@ -2,9 +2,9 @@
  * lyem_oracle.c -- CPU restatement of LyceanEM's raycasting + frequency-domain
  * propagation path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA library in
- * lyceanem-python_gb300/csrc: the parity tests, the smoke check and the CPU
- * baseline leg of bench.py call it.  Nothing in the product path links, loads
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA library in
+ * lyceanem-python_gb300/csrc is compared with: the parity tests, the smoke
+ * check and the CPU baseline leg of bench.py call it.  Nothing in the product path links, loads
  * or calls it.
  *
  * Two arithmetic modes:

@@ -1,7 +1,7 @@
 """NumPy front end of the CPU oracle (test infrastructure only).
 
-This module is the checker for the CUDA path: tests, the smoke check and the
-CPU-baseline leg of bench.py use it.  It is never imported by the product
+This module is the oracle the CUDA path is compared with: tests, the smoke
+check and the CPU-baseline leg of bench.py use it.  It is never imported by the product
 package.  Visibility is the bit-faithful FP32 restatement in lyem_oracle.c;
 fields are FP64.
 

@@ -102,4 +102,4 @@ def main(out_path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "reference_pairs.npz"))
+    main(sys.argv[1] if len(sys.argv) > 1 else "reference_pairs.npz")
