@@ -38,6 +38,8 @@ L2_FLUSH_BYTES = 256 << 20
 # one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (220.77 MB + 6.32 GB; the
 # writes are mostly the per-chunk partial sums).
 GRID_STAGE_DRAM_BYTES = 220.77e6 + 6.32e9
+# DRAM bytes of one launch of the brute-force kernel on the 8x8-array direct scene (profiles/brute_stage_kernel_direct.md)
+BRUTE_STAGE_DRAM_BYTES = 153.6e3
 
 
 def parse():
@@ -263,7 +265,9 @@ def run_ours(args, rank, world):
     achieved = tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12
     peak = fma_rate / 1e12
     res["roofline"] = {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                       "frac": achieved / peak, "traffic": GRID_STAGE_DRAM_BYTES,
+                       "frac": achieved / peak,
+                       "traffic": GRID_STAGE_DRAM_BYTES if args.workload == "bounce" else
+                       (BRUTE_STAGE_DRAM_BYTES if args.workload == "direct" else None),
                        "peak_source": "measured FP32 FMA lane-op rate (lyem_fp32_fma_probe, same run; FMA = 1 op)",
                        "tests_per_launch": tests, "ops_per_test": OPS_PER_TEST, "launch_ms": s2_ms,
                        "share_of_step": s2_ms / ms_per_step,
