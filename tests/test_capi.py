@@ -106,3 +106,17 @@ def test_header_compiles_as_c_and_links(tmp_path):
                     "-L", libdir, "-llyem_gpu", "-Wl,-rpath," + libdir], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert int(out[0]) >= 100 and out[-3:] == ["41", "41", "13"]
+
+
+def test_sweep_three_product_modes_host_checks():
+    """The Gauss sweep modes (3, 4) need a workspace: sized by lyem_sweep_workspace_bytes, refused by the
+    entry point without one, and refused by the workspace-less lyem_sweep_run (host checks, no device call)."""
+    from lyceanem_gb300._native import lib
+    assert lib.lyem_sweep_workspace_bytes(1024, 16, 3) == 3 * 1024 * 16 * 4
+    assert lib.lyem_sweep_workspace_bytes(1024, 16, 1) == 0
+    assert lib.lyem_sweep_network_bytes(10, 16, 3) == 3 * 6 * 16 * 10 * 2
+    assert lib.lyem_sweep_weights_bytes(10, 4, 4) == 9 * 10 * 4 * 2
+    fake = ctypes.c_void_p(256)
+    assert lib.lyem_sweep_run_ws(fake, 10, 16, 16, None, fake, 4, 3, fake, 16, None, 0, None) == 6  # workspace
+    assert lib.lyem_sweep_run(fake, 10, 16, 16, None, fake, 4, 3, fake, 16, None) == 1  # invalid: needs _ws
+    assert lib.lyem_sweep_run_ws(fake, 10, 16, 16, None, fake, 4, 5, fake, 16, None, 0, None) == 1  # no mode 5
