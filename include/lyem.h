@@ -100,11 +100,14 @@ LYEM_API int lyem_grid_count(const float *d_tris, int64_t n_tris, const float *o
 /* Uniform-grid build, phase 2: emits (cell, triangle) keys, radix-sorts them
  * by cell (stable, so triangles are ascending within a cell), writes the cell
  * ranges d_cell_start[ncells+1], the triangles in cell order
- * d_cell_tris[n_refs,12] and the traversal's cell table d_cell_box[ncells,8]
- * (16-byte aligned): per cell (lo.x, lo.y, lo.z, first ref, hi.x, hi.y, hi.z,
- * end ref), the refs stored as int32 bits and [lo, hi] the box of the cell's
- * triangles (padded as for the binning) within the cell widened by two pads;
- * a segment that misses it skips the cell's triangles.  Replaces bin_triangles_kernel_precounted /
+ * d_cell_tris[n_refs,12] and the traversal's cell table d_cell_box[ncells,16]
+ * (16-byte aligned).  Within a cell the triangles are split at the cell's
+ * centre (along the axis of largest centroid spread) into child A then child
+ * B, each in ascending triangle order; the record is (loA.xyz, first ref,
+ * hiA.xyz, first ref of B, loB.xyz, first ref of B, hiB.xyz, end ref), refs
+ * stored as int32 bits, each [lo, hi] the box of the child's triangles (padded
+ * as for the binning) within the cell widened by two pads; a segment that
+ * misses a child's box skips that child's triangles.  Replaces bin_triangles_kernel_precounted /
  * compute_bin_offsets / insert_triangle_in_bin
  * (lyceanem/src/terrain_acceleration_build.cuh:135-205, 349-368) and the host
  * prefix sum of lyceanem/src/frequency_domain_models.cu:118-123. */
@@ -284,7 +287,7 @@ typedef struct lyem_batch_scene {
     const int32_t *scat_id;    /* [n_scat] or NULL */
     const int32_t *cell_start; /* [cells + 1] */
     const float *cell_tris;    /* [refs, 12], 16-byte aligned */
-    const float *cell_box;     /* [cells, 8], 16-byte aligned (lyem_grid_fill) */
+    const float *cell_box;     /* [cells, 16], 16-byte aligned (lyem_grid_fill) */
     int64_t n_src;
     int64_t n_scat;
     float grid_origin[3];

@@ -542,7 +542,7 @@ int em_scatter(const float* source, int64_t n_source, const float* end, int64_t 
         const long long ncells = (long long)dims[0] * dims[1] * dims[2];
         LYEM_CK(dstart.alloc(sizeof(int) * (size_t)(ncells + 1), s));
         LYEM_CK(dcell.alloc(48 * (size_t)total, s));
-        LYEM_CK(dbox.alloc(32 * (size_t)ncells, s));
+        LYEM_CK(dbox.alloc(64 * (size_t)ncells, s));
         DevBuf dfw;
         LYEM_CK(dfw.alloc(grid_fill_workspace_bytes((long long)total, ncells), s));
         LYEM_CK(grid_fill(b, dt.as<float4>(), n_tris, doff.as<int>(), (long long)total, dstart.as<int>(),

@@ -10,8 +10,9 @@
 //   5. cell ranges by binary search of the sorted keys;
 //   6. gather the packed triangles into cell order (contiguous float4 loads
 //      for the traversal);
-//   7. per cell, the box of its triangles within the cell and its ref range
-//      (one 32-byte record per cell step of the traversal).
+//   7. per cell, its triangles split in two children at the cell's centre, each
+//      child's box within the cell and ref range (one 64-byte record per cell
+//      step of the traversal); steps 6 and 7 are one pass per cell.
 // This replaces the reference's vertex binning with device asserts, its
 // O(cells^2) single-block offset computation and its atomicCAS slot
 // insertion (lyceanem/src/terrain_acceleration_build.cuh:30-205, 287-431) and
@@ -329,42 +330,100 @@ __global__ void gather_tris_kernel(const float4* __restrict__ tris, const int* _
     }
 }
 
-// Cell table of the traversal: for cell c the union of the padded boxes of its
-// triangles (vertices and pad exactly as covered_range computes them), clipped
-// to the cell widened by two pads, and the cell's ref range.  A segment whose
-// exact path misses this box cannot hit a triangle of the cell inside the cell
-// (a hit point lies in its triangle's box and in the cell, at least a pad inside
-// the clipped box), and a hit outside the cell is found in the cell that holds it.
-// Empty cells get lo = +inf, hi = -inf.  Non-finite triangle coordinates are
+// Cell table of the traversal and the cell-ordered triangles, one thread per
+// cell.  A cell's triangles are split at the cell's centre along the axis of
+// largest centroid spread into two children, A (centroid below) then B, each
+// kept in the (ascending) triangle order of the sorted refs, and the record of
+// cell c is four float4:
+//   (loA.xyz, first ref) (hiA.xyz, first ref of B) (loB.xyz, first ref of B) (hiB.xyz, end ref)
+// (refs as int bits), [lo, hi] of a child being the union of the padded boxes of
+// its triangles (vertices and pad exactly as covered_range computes them),
+// clipped to the cell widened by two pads.  A segment whose exact path misses a
+// child's box cannot hit a triangle of that child inside the cell (a hit point
+// lies in its triangle's box and in the cell, at least a pad inside the clipped
+// box), and a hit outside the cell is found in the cell that holds it.  Empty
+// children get lo = +inf, hi = -inf.  Non-finite triangle coordinates are
 // ignored by fminf/fmaxf: such triangles never pass the ray-triangle test.
-__global__ void cell_box_kernel(BinSpec b, const int* __restrict__ cell_start, const float4* __restrict__ cell_tris,
-                                long long ncells, float4* __restrict__ box) {
+__device__ __forceinline__ void tri_box(const BinSpec& b, float4 v0, float4 e1, float4 e2, float lo[3], float hi[3]) {
+    const float a[3] = {v0.x, v0.y, v0.z}, e[3] = {e1.x, e1.y, e1.z}, f[3] = {e2.x, e2.y, e2.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float p = a[k], q = a[k] + e[k], s = a[k] + f[k];
+        lo[k] = fminf(lo[k], fminf(p, fminf(q, s)) - b.pad);
+        hi[k] = fmaxf(hi[k], fmaxf(p, fmaxf(q, s)) + b.pad);
+    }
+}
+
+__device__ __forceinline__ float tri_centroid(float4 v0, float4 e1, float4 e2, int k) {
+    const float a[3] = {v0.x, v0.y, v0.z}, e[3] = {e1.x, e1.y, e1.z}, f[3] = {e2.x, e2.y, e2.z};
+    return a[k] + (e[k] + f[k]) * (1.f / 3.f);
+}
+
+__global__ void cell_fill_kernel(BinSpec b, const float4* __restrict__ tris, const int* __restrict__ vals,
+                                 const int* __restrict__ cell_start, long long ncells, float4* __restrict__ cell_tris,
+                                 float4* __restrict__ box) {
     const long long plane = (long long)b.dims[0] * b.dims[1];
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncells;
          c += (long long)gridDim.x * blockDim.x) {
         const int q0 = cell_start[c], q1 = cell_start[c + 1];
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int r = q0; r < q1; ++r) {
-            const float4 v0 = cell_tris[3 * (long long)r], e1 = cell_tris[3 * (long long)r + 1],
-                         e2 = cell_tris[3 * (long long)r + 2];
-            const float a[3] = {v0.x, v0.y, v0.z}, e[3] = {e1.x, e1.y, e1.z}, f[3] = {e2.x, e2.y, e2.z};
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float p = a[k], q = a[k] + e[k], s = a[k] + f[k];
-                lo[k] = fminf(lo[k], fminf(p, fminf(q, s)) - b.pad);
-                hi[k] = fmaxf(hi[k], fmaxf(p, fmaxf(q, s)) + b.pad);
-            }
-        }
         const long long iz = c / plane, rem = c - iz * plane, iy = rem / b.dims[0], ix = rem - iy * b.dims[0];
         const float ci[3] = {(float)ix, (float)iy, (float)iz};
+        // split axis: largest spread of the centroids; split plane: the cell's centre on it
+        float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int r = q0; r < q1; ++r) {
+            const float4* t = tris + 3 * (long long)vals[r];
+            const float4 v0 = t[0], e1 = t[1], e2 = t[2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float x = tri_centroid(v0, e1, e2, k);
+                cmin[k] = fminf(cmin[k], x);
+                cmax[k] = fmaxf(cmax[k], x);
+            }
+        }
+        int ax = 0;
+        float spread = -1.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float d = cmax[k] - cmin[k];
+            if (d > spread) {
+                spread = d;
+                ax = k;
+            }
+        }
+        const float mid = b.org[ax] + (ci[ax] + 0.5f) * b.cell;
+        int na = 0;
+        for (int r = q0; r < q1; ++r) {
+            const float4* t = tris + 3 * (long long)vals[r];
+            na += tri_centroid(t[0], t[1], t[2], ax) < mid ? 1 : 0;
+        }
+        float loA[3] = {INFINITY, INFINITY, INFINITY}, hiA[3] = {-INFINITY, -INFINITY, -INFINITY};
+        float loB[3] = {INFINITY, INFINITY, INFINITY}, hiB[3] = {-INFINITY, -INFINITY, -INFINITY};
+        int ia = q0, ib = q0 + na;
+        for (int r = q0; r < q1; ++r) {
+            const float4* t = tris + 3 * (long long)vals[r];
+            const float4 v0 = t[0], e1 = t[1], e2 = t[2];
+            const bool in_a = tri_centroid(v0, e1, e2, ax) < mid;
+            const int o = in_a ? ia++ : ib++;
+            cell_tris[3 * (long long)o] = v0;
+            cell_tris[3 * (long long)o + 1] = e1;
+            cell_tris[3 * (long long)o + 2] = e2;
+            if (in_a) tri_box(b, v0, e1, e2, loA, hiA);
+            else tri_box(b, v0, e1, e2, loB, hiB);
+        }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const float c0 = b.org[k] + ci[k] * b.cell;
-            lo[k] = fmaxf(lo[k], c0 - 2.f * b.pad);
-            hi[k] = fminf(hi[k], c0 + b.cell + 2.f * b.pad);
+            const float clo = c0 - 2.f * b.pad, chi = c0 + b.cell + 2.f * b.pad;
+            loA[k] = fmaxf(loA[k], clo);
+            hiA[k] = fminf(hiA[k], chi);
+            loB[k] = fmaxf(loB[k], clo);
+            hiB[k] = fminf(hiB[k], chi);
         }
-        box[2 * c] = make_float4(lo[0], lo[1], lo[2], __int_as_float(q0));
-        box[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], __int_as_float(q1));
+        const int qm = q0 + na;
+        box[4 * c] = make_float4(loA[0], loA[1], loA[2], __int_as_float(q0));
+        box[4 * c + 1] = make_float4(hiA[0], hiA[1], hiA[2], __int_as_float(qm));
+        box[4 * c + 2] = make_float4(loB[0], loB[1], loB[2], __int_as_float(qm));
+        box[4 * c + 3] = make_float4(hiB[0], hiB[1], hiB[2], __int_as_float(q1));
     }
 }
 
@@ -586,10 +645,13 @@ cudaError_t grid_fill(const BinSpec& b, const float4* tris, long long n_tris, co
     const int* vals = nullptr;
     cudaError_t e = grid_sort(b, tris, n_tris, tri_offsets, n_refs, cell_start, &vals, ws, stream);
     if (e != cudaSuccess) return e;
-    if (n_refs > 0) { gather_tris_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tris, vals, n_refs, cell_tris); note_launches(1); }
+    const long long ncells = (long long)b.dims[0] * b.dims[1] * b.dims[2];
     if (cell_box) {
-        const long long ncells = (long long)b.dims[0] * b.dims[1] * b.dims[2];
-        cell_box_kernel<<<grid_blocks(ncells, 256), 256, 0, stream>>>(b, cell_start, cell_tris, ncells, cell_box);
+        cell_fill_kernel<<<grid_blocks(ncells, 128), 128, 0, stream>>>(b, tris, vals, cell_start, ncells, cell_tris,
+                                                                      cell_box);
+        note_launches(1);
+    } else if (n_refs > 0) {
+        gather_tris_kernel<<<grid_blocks(3 * n_refs, 256), 256, 0, stream>>>(tris, vals, n_refs, cell_tris);
         note_launches(1);
     }
     return cudaGetLastError();

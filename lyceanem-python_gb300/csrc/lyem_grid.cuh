@@ -32,10 +32,10 @@ cudaError_t grid_count(const BinSpec& b, const float4* tris, long long n_tris, i
                        unsigned long long* total, void* ws, cudaStream_t stream);
 
 size_t grid_fill_workspace_bytes(long long n_refs, long long n_cells);
-// Also writes the traversal's cell table cell_box[2 * ncells] (3-D grids only):
-// (lo.x, lo.y, lo.z, first ref) (hi.x, hi.y, hi.z, end ref), refs as int bits,
-// [lo, hi] = the union of the cell's padded triangle boxes (the boxes the
-// binning used) clipped to the cell widened by two pads.
+// Also writes the traversal's cell table cell_box[4 * ncells] (3-D grids only):
+// per cell two children (its triangles split at the cell centre), each with the
+// union of its padded triangle boxes (the boxes the binning used) clipped to the
+// cell widened by two pads, and its ref range (see cell_fill_kernel).
 cudaError_t grid_fill(const BinSpec& b, const float4* tris, long long n_tris, const int* tri_offsets, long long n_refs,
                       int* cell_start, float4* cell_tris, float4* cell_box, void* ws, cudaStream_t stream);
 cudaError_t bin_fill_index(const BinSpec& b, const float4* tris, long long n_tris, const int* tri_offsets,

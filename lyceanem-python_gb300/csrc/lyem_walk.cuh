@@ -19,19 +19,13 @@ struct Walk {
     int cx, cy, cz, q, q1, guard;
 };
 
-// Enters cell c: its ref range, emptied when the segment misses the box of
-// the cell's triangles.  Slab test over the parameter range [0, len] (the
-// cell's own range is a part of it); an axis the segment is parallel to only
-// checks the origin coordinate.  The computed slab parameters carry relative
-// errors of a few units of 2^-24, so the box counts as missed only when the
-// entry parameter exceeds the exit parameter by more than 2^-19 of it; NaN
-// parameters never make a miss.
-template <class GP>
-__device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
-    const float4 lo = __ldg(p.cell_box + 2 * (long long)c), hi = __ldg(p.cell_box + 2 * (long long)c + 1);
-    w.q = __float_as_int(lo.w);
-    w.q1 = __float_as_int(hi.w);
-    if (w.q >= w.q1) return;
+// True when the segment certainly misses box [lo, hi]: slab test over the
+// parameter range [0, len] (a cell's own range is a part of it); an axis the
+// segment is parallel to only checks the origin coordinate.  The computed slab
+// parameters carry relative errors of a few units of 2^-24, so the box counts
+// as missed only when the entry parameter exceeds the exit parameter by more
+// than 2^-19 of it; NaN parameters never make a miss.
+__device__ __forceinline__ bool box_missed(const Walk& w, float4 lo, float4 hi) {
     const float kInf = __int_as_float(0x7f800000);
     float tmin = 0.f, tmax = w.r.len;
     bool out = false;
@@ -47,7 +41,21 @@ __device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
     LYEM_BOX(w.r.dy, w.oy, w.iy, lo.y, hi.y)
     LYEM_BOX(w.r.dz, w.oz, w.iz, lo.z, hi.z)
 #undef LYEM_BOX
-    if (out || __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax) w.q = w.q1;
+    return out || __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax;
+}
+
+// Enters cell c: the ref range of the children whose boxes the segment may
+// cross (child A's refs come first, then B's, so the union is one range).
+template <class GP>
+__device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
+    const float4* rec = p.cell_box + 4 * (long long)c;
+    const float4 loA = __ldg(rec), hiA = __ldg(rec + 1);
+    const float4 loB = __ldg(rec + 2), hiB = __ldg(rec + 3);
+    int q = __float_as_int(loA.w), qm = __float_as_int(hiA.w), q1 = __float_as_int(hiB.w);
+    if (q < qm && box_missed(w, loA, hiA)) q = qm;
+    if (qm < q1 && box_missed(w, loB, hiB)) q1 = qm;
+    w.q = q;
+    w.q1 = q < q1 ? q1 : q;
 }
 
 // The segment o -> e of a walk (origin and ray); enough for walk_test_ref.
@@ -117,8 +125,8 @@ __device__ __forceinline__ int warp_nearest_ref(const GP& p, float ox, float oy,
     if (fx >= 0.f && fy >= 0.f && fz >= 0.f && fx < (float)p.dims[0] && fy < (float)p.dims[1] &&
         fz < (float)p.dims[2]) {
         const int c = ((int)fz * p.dims[1] + (int)fy) * p.dims[0] + (int)fx;
-        q0 = __float_as_int(__ldg(&p.cell_box[2 * (long long)c].w));
-        q1 = __float_as_int(__ldg(&p.cell_box[2 * (long long)c + 1].w));
+        q0 = __float_as_int(__ldg(&p.cell_box[4 * (long long)c].w));
+        q1 = __float_as_int(__ldg(&p.cell_box[4 * (long long)c + 3].w));
     }
     const int lane = threadIdx.x & 31;
     float best = __int_as_float(0x7f800000);

@@ -103,8 +103,9 @@ class UniformGrid:
         ncells = self.dims[0] * self.dims[1] * self.dims[2]
         self.cell_start = torch.empty(ncells + 1, dtype=torch.int32, device=dev)
         self.cell_tris = torch.empty((max(self.n_refs, 1), 12), dtype=torch.float32, device=dev)
-        # per cell: (lo.xyz, first ref) (hi.xyz, end ref), the box of the cell's triangles
-        self.cell_box = torch.empty((ncells, 8), dtype=torch.float32, device=dev)
+        # per cell two children (the cell's triangles split at its centre): (loA, first ref) (hiA, first ref
+        # of B) (loB, first ref of B) (hiB, end ref), each box that of the child's triangles within the cell
+        self.cell_box = torch.empty((ncells, 16), dtype=torch.float32, device=dev)
         ws2 = _ws(lib.lyem_grid_fill_workspace(self.n_refs, ncells), dev)
         check(lib.lyem_grid_fill(_p(tris), T, f32arr(self.origin), self.cell, i32arr(self.dims), _p(offsets),
                                  self.n_refs, _p(self.cell_start), _p(self.cell_tris), _p(self.cell_box), _p(ws2),

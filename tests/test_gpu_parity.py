@@ -188,23 +188,41 @@ def test_grid_build_matches_cpu_binning():
     start = g.cell_start.cpu().numpy()
     ct = g.cell_tris.cpu().numpy()
     assert start[-1] == g.n_refs == sum(len(c) for c in cells)
-    for c in range(g.n_cells):
-        got = ct[start[c]:start[c + 1]]
-        assert np.array_equal(got, t[cells[c]]), c
-    # cell table: ref range and the box of the cell's padded triangle boxes within the cell widened by 2 pads
+    # cell table: per cell child A (centroid below the cell centre on the axis of largest centroid spread) then
+    # child B, each in triangle order, with the box of its padded triangle boxes within the cell widened by 2 pads
     box = g.cell_box.cpu().numpy()
-    refs = np.ascontiguousarray(box[:, [3, 7]]).view(np.int32)
-    assert np.array_equal(refs[:, 0], start[:-1]) and np.array_equal(refs[:, 1], start[1:])
+    refs = np.ascontiguousarray(box[:, [3, 7, 11, 15]]).view(np.int32)
+    assert np.array_equal(refs[:, 0], start[:-1]) and np.array_equal(refs[:, 3], start[1:])
+    assert np.array_equal(refs[:, 1], refs[:, 2])
     pad = np.float32(1e-3) * np.float32(g.cell)
     vlo, vhi = vv.min(1) - pad, vv.max(1) + pad
+    cen = vv.astype(np.float64).mean(1)
     for c in range(g.n_cells):
-        if not cells[c]:
+        L = np.array(cells[c], dtype=int)
+        if not len(L):
             continue
         ix = np.array([c % g.dims[0], (c // g.dims[0]) % g.dims[1], c // (g.dims[0] * g.dims[1])])
         c0 = org + ix * np.float32(g.cell)
-        lo = np.maximum(vlo[cells[c]].min(0), c0 - 2 * pad)
-        hi = np.minimum(vhi[cells[c]].max(0), c0 + np.float32(g.cell) + 2 * pad)
-        assert np.allclose(box[c, 0:3], lo, rtol=0, atol=1e-5) and np.allclose(box[c, 4:7], hi, rtol=0, atol=1e-5), c
+        spread = cen[L].max(0) - cen[L].min(0)
+        ax = int(np.argmax(spread))
+        mid = org[ax] + (ix[ax] + 0.5) * g.cell
+        in_a = cen[L, ax] < mid
+        got = ct[start[c]:start[c + 1]]
+        na = refs[c, 1] - refs[c, 0]
+        assert sorted(map(tuple, got.tolist())) == sorted(map(tuple, t[L].tolist())), c
+        # the split rule, where FP32 and FP64 centroids cannot disagree (clear axis, no centroid at the plane)
+        clear_axis = np.sort(spread)[-1] - np.sort(spread)[-2] > 1e-4 if len(L) > 1 else True
+        if clear_axis and np.all(np.abs(cen[L, ax] - mid) > 1e-5):
+            assert np.array_equal(got[:na], t[L[in_a]]) and np.array_equal(got[na:], t[L[~in_a]]), c
+        for child, rows in ((0, got[:na]), (1, got[na:])):
+            lo_b, hi_b = box[c, 8 * child:8 * child + 3], box[c, 8 * child + 4:8 * child + 7]
+            if not len(rows):
+                assert np.all(np.isinf(lo_b)) and np.all(np.isinf(hi_b)), c
+                continue
+            rv = np.stack([rows[:, 0:3], rows[:, 0:3] + rows[:, 4:7], rows[:, 0:3] + rows[:, 8:11]], 1)
+            lo = np.maximum(rv.min(1).min(0) - pad, c0 - 2 * pad)
+            hi = np.minimum(rv.max(1).max(0) + pad, c0 + np.float32(g.cell) + 2 * pad)
+            assert np.allclose(lo_b, lo, rtol=0, atol=1e-5) and np.allclose(hi_b, hi, rtol=0, atol=1e-5), c
 
 
 def test_bounce_scene_reduced_vs_oracle():
