@@ -49,11 +49,18 @@ __device__ __forceinline__ bool box_missed(const Walk& w, float4 lo, float4 hi) 
 template <class GP>
 __device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
     const float4* rec = p.cell_box + 4 * (long long)c;
-    const float4 loA = __ldg(rec), hiA = __ldg(rec + 1);
-    const float4 loB = __ldg(rec + 2), hiB = __ldg(rec + 3);
-    int q = __float_as_int(loA.w), qm = __float_as_int(hiA.w), q1 = __float_as_int(hiB.w);
-    if (q < qm && box_missed(w, loA, hiA)) q = qm;
-    if (qm < q1 && box_missed(w, loB, hiB)) q1 = qm;
+    int q, qm, q1;
+    {
+        const float4 loA = __ldg(rec), hiA = __ldg(rec + 1);
+        q = __float_as_int(loA.w);
+        qm = __float_as_int(hiA.w);
+        if (q < qm && box_missed(w, loA, hiA)) q = qm;
+    }
+    {
+        const float4 loB = __ldg(rec + 2), hiB = __ldg(rec + 3);
+        q1 = __float_as_int(hiB.w);
+        if (qm < q1 && box_missed(w, loB, hiB)) q1 = qm;
+    }
     w.q = q;
     w.q1 = q < q1 ? q1 : q;
 }
