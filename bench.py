@@ -35,9 +35,9 @@ METRIC = "visible paths/s (mask+field) on 1 GB300; mixed-prec vs FP32 sweep at â
 OPS_PER_TEST = 30  # FP32-pipe operations of one Moller-Trumbore test (lyceanem/src/raycasting.cuh:23-59)
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (read + write) of one full-size launch of the scatter->sink grid-stage kernel, from the
-# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (400.24 MB + 10.72 GB; the
+# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (217.43 MB + 6.39 GB; the
 # writes are the per-chunk partial sums and spill lines written back).
-GRID_STAGE_DRAM_BYTES = 400.24e6 + 10.72e9
+GRID_STAGE_DRAM_BYTES = 217.43e6 + 6.39e9
 # DRAM bytes of one launch of the brute-force kernel on the 8x8-array direct scene (profiles/brute_stage_kernel_direct.md)
 BRUTE_STAGE_DRAM_BYTES = 153.6e3
 
