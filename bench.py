@@ -34,12 +34,24 @@ sys.path.insert(0, ROOT)
 METRIC = "visible paths/s (mask+field) on 1 GB300; mixed-prec vs FP32 sweep at ≤1e-4 rel err"
 OPS_PER_TEST = 30  # FP32-pipe operations of one Moller-Trumbore test (lyceanem/src/raycasting.cuh:23-59)
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (read + write) of one full-size launch of the scatter->sink grid-stage kernel, from the
-# one-pass ncu capture summarised in profiles/grid_stage_kernel_bounce.md (217.43 MB + 6.39 GB; the
-# writes are the per-chunk partial sums and spill lines written back).
-GRID_STAGE_DRAM_BYTES = 217.43e6 + 6.39e9
-# DRAM bytes of one launch of the brute-force kernel on the 8x8-array direct scene (profiles/brute_stage_kernel_direct.md)
-BRUTE_STAGE_DRAM_BYTES = 153.6e3
+# sample strides of the CPU legs and of the parity leg: every k-th sink and scatter point, all sources
+# (the direct workload is small enough to run whole)
+CPU_STRIDES = (16, 11)
+CPU_STRIDES_DIRECT = (1, 2)
+PARITY_STRIDE = 16
+# DRAM traffic (read + write bytes per launch) of the dominant kernels, from one-pass ncu captures of
+# committed builds; each entry names its capture command and the commit it was measured on
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic.json")
+
+
+def traffic_record(workload):
+    """The recorded DRAM traffic of the dominant kernel of `workload` (dict with bytes, kernel, command,
+    commit) or None."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            return json.load(f).get(workload)
+    except (OSError, ValueError):
+        return None
 
 
 def parse():
@@ -63,7 +75,7 @@ def parse():
                     help="fg,chunk,blocks_per_sm for the batched launch instead of the autotuner (profiling cases)")
     ap.add_argument("--batched-cell-scale", type=float, default=0.0,
                     help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of the sampled baseline")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
     return ap.parse_args()
 
 
@@ -87,8 +99,13 @@ def describe(s, name):
     else:
         wl = ("direct + one bounce, 28 GHz, 32x32 array, 80,000 ground + 40,000 clutter triangles, "
               "50,000 scatter points, 65,341 sinks at 100 m, 0.5 m grid")
-    return {"workload": wl, "n_sources": N, "n_scatter": P, "n_sinks": M, "n_triangles": T, "paths_per_step": paths,
-            "grid_cell_m": s.cell, "l2": "flushed by a 256 MiB device write before every timed step"}, paths
+    cfg = {"workload": wl, "n_sources": N, "n_scatter": P, "n_sinks": M, "n_triangles": T, "paths_per_step": paths,
+           "grid_cell_m": s.cell, "l2": "flushed by a 256 MiB device write before every timed step"}
+    if P:
+        cfg["path_count"] = ("N*M direct pairs + N*P*M source-scatter-sink triples, the triples counted "
+                             "algebraically: the fused composition traces N*M + N*P + P*M rays and never forms a "
+                             "triple (rays_per_s and visible_paths_per_s are reported beside the value)")
+    return cfg, paths
 
 
 # ------------------------------------------------------------------ clocks
@@ -264,10 +281,12 @@ def run_ours(args, rank, world):
         kernel = "brute_stage_kernel (whole step)"
     achieved = tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12
     peak = fma_rate / 1e12
+    tr = traffic_record(args.workload)
     res["roofline"] = {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                        "frac": achieved / peak,
-                       "traffic": GRID_STAGE_DRAM_BYTES if args.workload == "bounce" else
-                       (BRUTE_STAGE_DRAM_BYTES if args.workload == "direct" else None),
+                       "traffic": tr["bytes"] if tr else None,
+                       "traffic_source": ({k: tr[k] for k in ("kernel", "command", "commit") if k in tr}
+                                          if tr else "no capture recorded"),
                        "peak_source": "measured FP32 FMA lane-op rate (lyem_fp32_fma_probe, same run; FMA = 1 op)",
                        "tests_per_launch": tests, "ops_per_test": OPS_PER_TEST, "launch_ms": s2_ms,
                        "share_of_step": s2_ms / ms_per_step,
@@ -276,6 +295,8 @@ def run_ours(args, rank, world):
                        "effective_frac": brute_tests * OPS_PER_TEST / (s2_ms / 1e3) / 1e12 / peak}
     if clk:
         res["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_parity:
+        res["parity"] = run_parity(args, s)
     if rank == 0 and world == 1 and not args.no_sweep:
         res["sweep"] = run_sweep(args)
     if rank == 0 and world == 1 and not args.no_adjoint:
@@ -295,6 +316,7 @@ def run_e2e(args, s, paths):
     import torch
 
     from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import acceleration_structures as AS
     from lyceanem_gb300.models import frequency_domain as FD
     beta = 2 * np.pi / s.wavelength
     solid = Mesh(s.verts, [("triangle", s.faces)])
@@ -305,6 +327,7 @@ def run_e2e(args, s, paths):
     axis = np.array([1.0, 0.0, 0.0])
 
     def call():
+        AS.clear_cache()  # every call uploads the mesh and builds its grid, as a first call on a scene does
         return FD.calculate_scattering(ap, sk, solid, axis, scatter_points=sc, wavelength=s.wavelength,
                                        scattering=scattering, beta=beta, cuda=True, grid_cell=s.cell)
 
@@ -318,11 +341,13 @@ def run_e2e(args, s, paths):
     V, T = s.verts.shape[0], s.faces.shape[0]
     h2d = (3 * (V * 12 + T * 12) + s.src.nbytes + s.src.shape[0] * 24 + s.snk.nbytes + s.snk_n.nbytes
            + s.scat.nbytes + s.scat_n.nbytes)
-    d2h = Ex.nbytes + Ey.nbytes + Ez.nbytes
+    # the reference-shaped tile structure built in the call reads its y-z bins back to the host
+    tile = next(iter(AS._CACHE.values()))
+    d2h = Ex.nbytes + Ey.nbytes + Ez.nbytes + tile.bin_counts.nbytes + tile.binned_triangles.nbytes
     return {"value": paths / dt, "unit": "paths/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "seconds_per_step": dt,
-            "api": "lyceanem_gb300.models.frequency_domain.calculate_scattering (host numpy in/out, "
-                   "acceleration structure built inside the call)"}
+            "api": "lyceanem_gb300.models.frequency_domain.calculate_scattering (host numpy in/out; the scene "
+                   "cache is cleared before every call, so each call uploads the mesh and builds the grid)"}
 
 
 # ------------------------------------------------------------------ sweep
@@ -478,6 +503,7 @@ def run_batched(args, reps=2):
             ref = out.cpu().numpy()
             worst = max(worst, float(np.abs(field[si, f].cpu().numpy() - ref).max() / np.abs(ref).max()))
     res["rel_err_vs_pair_stages"] = worst
+    res["fp64_check_large"] = batched_fp64_check(bs, scenes, snk, snk_n, freqs)
     # FP64 oracle (brute-force visibility on the host) on the scene with the fewest ray-triangle tests,
     # first and last frequency; skipped when even that scene is too large for a bounded CPU check
     costs = [(d.src.shape[0] * (bs.n_snk + d.scat.shape[0]) + d.scat.shape[0] * bs.n_snk) * d.n_tris for d in bs.data]
@@ -501,6 +527,51 @@ def run_batched(args, reps=2):
     res["oracle_scene"] = {"index": si, "elements": int(sc.src.shape[0]), "scatter": int(sc.scat.shape[0]),
                            "triangles": int(sc.faces.shape[0])}
     return res
+
+
+def batched_fp64_check(bs, scenes, snk, snk_n, freqs, n_snk=500, n_scat=600, freq_idx=None):
+    """The batched kernel against the FP64 oracle on the scenes with the most triangles and with the most
+    elements, each on a sample of its scatter points and of the sinks (every k-th), all sources, the full
+    mesh, with the launch configuration and grid rule of `bs`; relative error per checked frequency (the
+    first, a middle and the last, where the kernel's per-group phase rotation has run longest)."""
+    import numpy as np
+
+    from lyceanem_gb300 import batched as B
+    from oracle import oracle as O
+    if freq_idx is None:
+        freq_idx = sorted({0, len(freqs) // 2 + 1, len(freqs) - 1})
+    picks = sorted({int(np.argmax([sc.faces.shape[0] for sc in scenes])),
+                    int(np.argmax([sc.src.shape[0] for sc in scenes]))})
+    ks = max(1, snk.shape[0] // n_snk)
+    ys, yn = snk[::ks], snk_n[::ks]
+    out = []
+    for si in picks:
+        sc = scenes[si]
+        kp = max(1, sc.scat.shape[0] // n_scat)
+        scat, scat_n = sc.scat[::kp], sc.scat_n[::kp]
+        sub = dict(src=sc.src, verts=sc.verts, faces=sc.faces, scat=scat, scat_n=scat_n)
+        cb = B.BatchedScattering([sub], ys, yn, freqs, cell_scale=bs.cell_scale or 1.0, config=bs.config)
+        field = cb.run().cpu().numpy()[0]
+        og = O.Grid(O.pack_triangles(sc.verts, sc.faces), 0.5)
+        m0, m1, m2 = og.mask(sc.src, ys), og.mask(sc.src, scat), og.mask(scat, ys)
+        E = np.tile(np.array([[1, 0, 0]], np.complex64), (sc.src.shape[0], 1))
+        errs = []
+        for f in freq_idx:
+            b_ = float(cb.betas[f])
+            e = O.sink_field(sc.src, E, ys, yn, 0.0, b_, mask=m0)
+            ep = O.sink_field(sc.src, E, scat, scat_n, 0.0, b_, mask=m1)
+            e = e + O.sink_field(scat, ep, ys, yn, 0.0, b_, srcW=ep, mask=m2)
+            errs.append(float(np.abs(field[f] - e).max() / np.abs(e).max()))
+        pts = np.concatenate([sc.src, scat]).astype(np.float64)
+        rmax = float(np.sqrt(((ys.astype(np.float64)[None] - pts[:, None]) ** 2).sum(-1)).max())
+        out.append({"scene": si, "elements": int(sc.src.shape[0]), "triangles": int(sc.faces.shape[0]),
+                    "scatter_sampled": int(scat.shape[0]), "sinks_sampled": int(ys.shape[0]),
+                    "freq_index": [int(f) for f in freq_idx], "rel_err_per_freq": errs,
+                    "max_kr_rad": float(cb.betas.max()) * rmax,
+                    "visible_pairs": [int(m0.sum()), int(m1.sum()), int(m2.sum())]})
+        del cb
+    return {"metric": "max |E - E_fp64| / max |E_fp64| per frequency over the sampled sinks and components",
+            "scenes": out, "max_rel_err": max(e for o in out for e in o["rel_err_per_freq"])}
 
 
 # ------------------------------------------------------------------ adjoint
@@ -603,6 +674,81 @@ def run_adjoint(args, reps=3):
                         "error = |grad - fd| / max|grad| over 4 excitation and 2 position components"}
 
 
+# ------------------------------------------------------------------ parity
+def run_parity(args, s):
+    """Parity of the benchmarked workload at full geometry: the step's stages (same kernels, orders and
+    grid) run on every PARITY_STRIDE-th sink and scatter point with all sources and the full mesh (the
+    direct workload runs whole); each stage's mask is compared bit for bit with the oracle's, mismatching
+    pairs are classified as epsilon-edge cases by an FP64 re-test, and the sink field of the sample is
+    compared with the FP64 oracle's field on the oracle's masks.  Reference behaviour:
+    lyceanem/src/raycasting.cuh:19-95, lyceanem/src/em.cuh:18-120, composed as
+    lyceanem/models/frequency_domain.py:195-264, 847-849."""
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300 import propagation as P
+    from oracle import oracle as O
+    dev = torch.device("cuda")
+    beta = 2 * np.pi / s.wavelength
+    k = 1 if args.workload == "direct" else PARITY_STRIDE
+    snk, snk_n = s.snk[::k], s.snk_n[::k]
+    scat, scat_n = s.scat[::k], s.scat_n[::k]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    tris = P.pack_triangles(t(s.verts), t(s.faces))
+    t12 = O.pack_triangles(s.verts, s.faces)
+    if args.workload == "direct":
+        grid = og = None
+        kw = dict(beta=beta, tris=tris)
+    else:
+        grid = P.UniformGrid(tris, cell=s.cell)
+        og = O.Grid(t12, s.cell)
+        kw = dict(beta=beta, grid=grid)
+    src, E = t(s.src), t(s.E)
+    yk, ykn = t(snk), t(snk_n)
+    o_snk = P.direction_order(yk, grid.centre) if grid is not None else None
+    r0 = P.pair_stage(src, E, yk, ykn, want_mask=True, snk_order=o_snk, **kw)
+    field = r0.sink.clone()
+    stages = [("direct", s.src, snk, r0)]
+    if scat.shape[0]:
+        pk, pkn = t(scat), t(scat_n)
+        o_scat = P.spatial_order(pk)
+        r1 = P.pair_stage(src, E, pk, pkn, want_mask=True, snk_order=o_scat, **kw)
+        e_p = r1.sink
+        r2 = P.pair_stage(pk, e_p, yk, ykn, src_W=e_p, sink_out=field, accumulate=True, want_mask=True,
+                          src_order=o_scat, snk_order=o_snk, **kw)
+        stages += [("source_scatter", s.src, scat, r1), ("scatter_sink", scat, snk, r2)]
+    gpu_masks = {name: r.mask().cpu().numpy() for name, _, _, r in stages}
+    field = field.cpu().numpy()
+    st, flags = P.device_errors()
+    res = {"sample": (f"every {k}th sink ({snk.shape[0]}) and scatter point ({scat.shape[0]}), all "
+                      f"{s.src.shape[0]} sources, all {s.faces.shape[0]} triangles"
+                      + (f", the bench's {s.cell} m grid" if grid is not None else ", brute force")),
+           "stages": {}, "device_errors": [int(st), int(flags)]}
+    om = {}
+    mism = edge = pairs_total = 0
+    for name, a, b, _ in stages:
+        m = (og.mask(a, b) if og is not None else O.mask_brute(a, b, t12)).astype(bool)
+        om[name] = m
+        bad = np.argwhere(gpu_masks[name] != m)
+        checked = bad[:200]
+        n_edge = int(O.edge_pairs(a, b, checked, t12).sum()) if len(checked) else 0
+        res["stages"][name] = {"pairs": int(m.size), "visible": int(m.sum()), "mask_mismatches": int(len(bad)),
+                               "edge_pairs": n_edge, "mismatches_classified": int(len(checked))}
+        mism += len(bad)
+        edge += n_edge
+        pairs_total += m.size
+    E64 = O.sink_field(s.src, s.E, snk, snk_n, 0.0, beta, mask=om["direct"])
+    if scat.shape[0]:
+        ep64 = O.sink_field(s.src, s.E, scat, scat_n, 0.0, beta, mask=om["source_scatter"])
+        E64 = E64 + O.sink_field(scat, ep64, snk, snk_n, 0.0, beta, srcW=ep64, mask=om["scatter_sink"])
+    err = float(np.abs(field - E64).max() / np.abs(E64).max())
+    res.update({"pairs": int(pairs_total), "mask_mismatches": int(mism), "edge_pairs": int(edge),
+                "field_rel_err": err, "field_tol": 1e-5,
+                "field_metric": "max |E_gpu - E_fp64| / max |E_fp64| over the sample's sinks and components",
+                "ok": bool(mism == edge and err <= 1e-5 and st == 0 and flags == 0)})
+    return res
+
+
 # ------------------------------------------------------------------ CPU
 def cpu_sample(s, stride_snk, stride_scat, nthreads):
     """Times the oracle on every stride-th sink / scatter point; returns per-stage seconds."""
@@ -631,55 +777,80 @@ def cpu_sample(s, stride_snk, stride_scat, nthreads):
     return dict(build=t_build, direct=t_direct, s1=t_s1, s2=t_s2, n_snk=snk.shape[0], n_scat=scat.shape[0])
 
 
-def cpu_extrapolate(s, paths, nthreads, target_s):
-    """Calibrate a sample size for ~target_s of CPU work, time it, extrapolate per stage to the full workload."""
+def cpu_extrapolate(s, paths, nthreads, stride):
+    """Times the oracle on every stride-th sink and scatter point (all sources, full mesh and grid) and
+    extrapolates stage by stage to the full workload.  Returns (paths/s of the full step, record)."""
     M, P = s.snk.shape[0], s.scat.shape[0]
-    cal = cpu_sample(s, 256, 256, nthreads)
-    # direct and source->scatter work scale with 1/stride, scatter->sink with 1/stride^2
-    stride = 256
-    while stride > 1:
-        nxt = stride // 2
-        est = (cal["direct"] + cal["s1"]) * (256 / nxt) + cal["s2"] * (256 / nxt) ** 2
-        if est > target_s:
-            break
-        stride = nxt
     r = cpu_sample(s, stride, stride, nthreads)
-    full = (r["build"] + r["direct"] * M / r["n_snk"]
-            + (r["s1"] * P / r["n_scat"] + r["s2"] * (P * M) / (r["n_scat"] * r["n_snk"]) if r["n_scat"] else 0.0))
+    f_direct = M / r["n_snk"]
+    f_s1 = P / r["n_scat"] if r["n_scat"] else 0.0
+    f_s2 = (P * M) / (r["n_scat"] * r["n_snk"]) if r["n_scat"] else 0.0
+    full = r["build"] + r["direct"] * f_direct + r["s1"] * f_s1 + r["s2"] * f_s2
     sample_s = r["build"] + r["direct"] + r["s1"] + r["s2"]
-    desc = (f"oracle (FP32 bit-faithful visibility on a CPU uniform grid, FP64 field) on every {stride}th sink "
-            f"({r['n_snk']}) and scatter point ({r['n_scat']}) with all {s.src.shape[0]} sources; "
-            f"{sample_s:.1f} s measured, extrapolated per stage (direct x M/M', source->scatter x P/P', "
-            f"scatter->sink x PM/(P'M')) to {full:.1f} s for the full step")
-    return paths / full, desc, full
+    N = s.src.shape[0]
+    rec = {"stride": stride, "n_sinks": r["n_snk"], "n_scatter": r["n_scat"], "sample_s": sample_s,
+           "stage_s": {k: r[k] for k in ("build", "direct", "s1", "s2")},
+           "extrapolation": {"direct": f_direct, "source_scatter": f_s1, "scatter_sink": f_s2},
+           "extrapolated_full_step_s": full, "paths_per_s": paths / full,
+           "rays_per_s": {"direct": N * r["n_snk"] / r["direct"] if r["direct"] else None,
+                          "source_scatter": N * r["n_scat"] / r["s1"] if r["s1"] else None,
+                          "scatter_sink": r["n_scat"] * r["n_snk"] / r["s2"] if r["s2"] else None}}
+    return paths / full, rec
+
+
+def cpu_describe(s, rec):
+    return (f"oracle (FP32 bit-faithful visibility on a CPU uniform grid, FP64 field) on every {rec['stride']}th "
+            f"sink ({rec['n_sinks']}) and scatter point ({rec['n_scatter']}) with all {s.src.shape[0]} sources, "
+            f"the full mesh and grid; {rec['sample_s']:.2f} s measured, extrapolated stage by stage "
+            f"(direct x M/M', source->scatter x P/P', scatter->sink x PM/(P'M')) to "
+            f"{rec['extrapolated_full_step_s']:.1f} s for the full step")
+
+
+def cpu_strides(args):
+    return CPU_STRIDES_DIRECT if args.workload == "direct" else CPU_STRIDES
 
 
 def cpu_baseline(args, s, paths):
+    """The oracle port on all host cores, on two sample sizes of the same workload (CPU_STRIDES); the
+    value is the larger sample's extrapolated rate, the other is reported beside it."""
     from oracle import oracle as O
     n = O.max_threads()
-    value, desc, _ = cpu_extrapolate(s, paths, n, args.cpu_seconds)
-    return {"value": value, "unit": "paths/s", "cores": n, "kind": "port", "sample": desc}
+    recs = [cpu_extrapolate(s, paths, n, k)[1] for k in cpu_strides(args)]
+    main = max(recs, key=lambda r: r["sample_s"])
+    rates = [r["paths_per_s"] for r in recs]
+    return {"value": main["paths_per_s"], "unit": "paths/s", "cores": n, "kind": "port",
+            "sample": cpu_describe(s, main), "samples": recs,
+            "stride_spread": max(rates) / min(rates) - 1.0}
 
 
 def run_reference(args, rank, world):
-    """CPU restatement of the path on the host cores (the reference has no CPU engine)."""
+    """CPU restatement of the path on the host cores (the reference has no CPU engine).  Each step is one
+    bounded sample (every CPU_STRIDES[0]-th sink and scatter point, all sources, the full mesh and grid),
+    timed and extrapolated stage by stage; ms_per_step is the measured sample time.  After the timed
+    steps the second sample size is measured once and reported beside the first."""
     from oracle import oracle as O
     s = workload_scene(args.workload)
     cfg, paths = describe(s, args.workload)
     n = O.max_threads()
-    vals, descs, fulls = [], [], []
-    for _ in range(max(1, args.steps)):
-        v, d, full = cpu_extrapolate(s, paths, n, args.cpu_seconds / max(1, args.steps))
-        vals.append(v)
-        descs.append(d)
-        fulls.append(full)
-    value = len(vals) / sum(1.0 / v for v in vals)
-    ms = 1e3 * sum(fulls) / len(fulls)
+    strides = cpu_strides(args)
+    stride = strides[0]
+    for _ in range(args.warmup):
+        cpu_extrapolate(s, paths, n, stride)
+    recs = [cpu_extrapolate(s, paths, n, stride)[1] for _ in range(max(1, args.steps))]
+    other = cpu_extrapolate(s, paths, n, strides[1])[1]
+    value = len(recs) / sum(1.0 / r["paths_per_s"] for r in recs)
+    ms = 1e3 * sum(r["sample_s"] for r in recs) / len(recs)
+    full_ms = 1e3 * sum(r["extrapolated_full_step_s"] for r in recs) / len(recs)
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 visibility / f64 field (CPU)", "data": "synthetic",
-            "config": cfg,
-            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": n, "kind": "port", "sample": descs[-1]},
+            "config": cfg, "extrapolated_full_step_ms": full_ms,
+            "step": "one sample of the workload per step (ms_per_step is its measured time); value = full-step "
+                    "paths / the sample's stage-by-stage extrapolated full-step time",
+            "cpu_baseline": {"value": value, "unit": "paths/s", "cores": n, "kind": "port",
+                             "sample": cpu_describe(s, recs[-1]), "samples": [recs[-1], other],
+                             "stride_spread": max(value, other["paths_per_s"]) /
+                             min(value, other["paths_per_s"]) - 1.0},
             "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

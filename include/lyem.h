@@ -189,10 +189,13 @@ LYEM_API int lyem_pair_stage(const float *d_src_pos, const float *d_src_E, const
  * fixed array inside the library of lyem_pair_stage_noalloc_scratch_bytes()
  * (32 MiB) on every device that loads it.  Limit: the per-chunk partial sums,
  * ceil(n_src / src_chunk) * n_snk * 24 bytes, must fit in it (src_chunk at most
- * 32 for brute force, 64 for the grid; with src_chunk = 0 the smallest chunk
- * that fits is used); larger problems return LYEM_ERR_WORKSPACE and launch
- * nothing.  The first call on a device looks up the array's device address
- * and should come before any stream capture.  All calls share the array (it
+ * 32 for brute force, 64 for the grid; with src_chunk = 0 the automatic
+ * chunk of lyem_pair_stage is used when its partial sums fit, else the
+ * smallest larger chunk whose partial sums fit); larger problems return
+ * LYEM_ERR_WORKSPACE and launch nothing.  Each call looks up the array's
+ * device address in the current device's context (so a device reset between
+ * calls is harmless); the first call on a device loads the library's device
+ * code there and should come before any stream capture.  All calls share the array (it
  * keeps the last call's contents; nothing in it needs to start at zero), so
  * calls that overlap on the GPU race.  Calls no allocation routine. */
 LYEM_API size_t lyem_pair_stage_noalloc_scratch_bytes(void);

@@ -265,10 +265,7 @@ __global__ void finish_source_kernel(const float* __restrict__ acc, const float*
     }
 }
 
-unsigned blocks_1d(long long n) {
-    long long b = (n + 255) / 256;
-    return (unsigned)(b < 1 ? 1 : (b > 152 * 16 ? 152 * 16 : b));
-}
+unsigned blocks_1d(long long n) { return capped_blocks(n, 256, 16); }
 
 long long chunks_of(long long n) { return (n + kAdjChunk - 1) / kAdjChunk; }
 

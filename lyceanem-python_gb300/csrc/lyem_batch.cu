@@ -617,13 +617,6 @@ void beta_tables(const double* beta, int n, std::vector<float2>& ff, std::vector
     uniform = dev <= 1e-12 * std::max(bmax, 1.0);
 }
 
-int sm_count() {
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    return n;
-}
-
 template <bool CULL, int FG, int MINB>
 cudaError_t launch_batch_t(const BatchParams& P, int blocks_per_sm, cudaStream_t stream, int* blocks_out) {
     auto kern = batch_kernel<CULL, FG, MINB>;
@@ -634,7 +627,7 @@ cudaError_t launch_batch_t(const BatchParams& P, int blocks_per_sm, cudaStream_t
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, kBT, smem);
     if (e != cudaSuccess) return e;
     const int per_sm = blocks_per_sm > 0 ? std::min(blocks_per_sm, std::max(fit, 1)) : std::max(fit, 1);
-    const int sms = sm_count();
+    const int sms = device_sm_count();
     if (sms <= 0) return cudaErrorInvalidDevice;
     const int blocks = std::max(1, std::min(per_sm * sms, P.n_items));
     kern<<<blocks, kBT, smem, stream>>>(P);

@@ -62,10 +62,7 @@ __global__ void mask_to_bytes_kernel(const unsigned* __restrict__ bits, long lon
     }
 }
 
-unsigned blocks_for(long long n, int threads, long long cap = 152LL * 32) {
-    long long b = (n + threads - 1) / threads;
-    return (unsigned)std::max(1LL, std::min(b, cap));
-}
+unsigned blocks_for(long long n, int threads) { return capped_blocks(n, threads, 32); }
 
 BinSpec grid_spec(const float* origin3, float cell, const int32_t* dims3) {
     BinSpec b;
@@ -88,24 +85,6 @@ bool valid_grid(const float* origin3, float cell, const int32_t* dims3) {
         nc *= dims3[k];
     }
     return nc < (1LL << 30);
-}
-
-// Sources per thread block when the caller passes 0.  Brute force: as many
-// as keep about four waves of blocks in flight (the triangle tiles are
-// re-staged per block).  Grid: 16, measured flat between 8 and 32 on the
-// 28 GHz one-bounce scene, fewer when that would leave under four waves.
-int auto_src_chunk(long long n_src, long long n_snk, bool grid) {
-    const long long tiles = (n_snk + stage_block_threads() - 1) / stage_block_threads();
-    const long long waves = 152LL * 8 * 4;
-    long long c;
-    if (grid) {
-        c = 16;
-        while (c > 1 && ((n_src + c - 1) / c) * tiles < waves) c /= 2;
-    } else {
-        c = (n_src * tiles) / waves;
-    }
-    const long long cap = grid ? grid_max_src_chunk() : brute_max_src_chunk();
-    return (int)std::max(1LL, std::min(c, cap));
 }
 
 size_t stage_ws_bytes(long long n_src, long long n_snk, int chunk) {
@@ -131,6 +110,25 @@ struct DevBuf {
 }  // namespace
 
 void lyem::record_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
+
+// Sources per thread block when the caller passes 0.  Brute force: as many
+// as keep about four waves of blocks in flight (the triangle tiles are
+// re-staged per block).  Grid: 16, measured flat between 8 and 32 on the
+// 28 GHz one-bounce scene, fewer when that would leave under four waves.
+int lyem::auto_src_chunk(long long n_src, long long n_snk, bool grid) {
+    const long long tiles = (n_snk + stage_block_threads() - 1) / stage_block_threads();
+    const long long waves = (long long)device_sm_count() * 8 * 4;
+    long long c;
+    if (grid) {
+        c = 16;
+        while (c > 1 && ((n_src + c - 1) / c) * tiles < waves) c /= 2;
+    } else {
+        c = (n_src * tiles) / waves;
+    }
+    const long long cap = grid ? grid_max_src_chunk() : brute_max_src_chunk();
+    return (int)std::max(1LL, std::min(c, cap));
+}
+
 
 extern "C" {
 

@@ -88,9 +88,8 @@ __global__ void bounds_decode_kernel(float* bounds6) {
 
 cudaError_t launch_tris_bounds(const float4* tris, long long n_tris, float* bounds6, cudaStream_t stream) {
     bounds_init_kernel<<<1, 32, 0, stream>>>(bounds6); note_launches(1);
-    long long blocks = (n_tris + 255) / 256;
-    blocks = blocks < 1 ? 1 : (blocks > 152 * 8 ? 152 * 8 : blocks);
-    tris_bounds_kernel<<<(unsigned)blocks, 256, 0, stream>>>(tris, n_tris, bounds6); note_launches(1);
+    const unsigned blocks = capped_blocks(n_tris, 256, 8);
+    tris_bounds_kernel<<<blocks, 256, 0, stream>>>(tris, n_tris, bounds6); note_launches(1);
     bounds_decode_kernel<<<1, 32, 0, stream>>>(bounds6); note_launches(1);
     return cudaGetLastError();
 }
@@ -537,13 +536,12 @@ cudaError_t direction_order(const float* pts, long long n, const float* centre3,
     int* hist = v1 + n + 64;
     int* hist_scanned = hist + 256 * nblocks + 64;
     int* scan_ws = hist_scanned + 256 * nblocks + 64;
-    long long b = (n + 255) / 256;
-    b = b > 152 * 8 ? 152 * 8 : b;
+    const unsigned b = capped_blocks(n, 256, 8);
     // tiles of about 16 points if the set were an even elevation-azimuth grid (n points over pi x 2 pi)
     const double kPi = 3.14159265358979323846;
     const double tile = std::max(0.009, 4.0 * std::sqrt(2.0 * kPi * kPi / (double)n));
     const int nb = (int)std::ceil(kPi / tile) + 2, na = (int)std::ceil(2.0 * kPi / tile) + 2;
-    direction_key_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, centre3[0], centre3[1], centre3[2], (float)tile,
+    direction_key_kernel<<<b, 256, 0, stream>>>(pts, n, centre3[0], centre3[1], centre3[2], (float)tile,
                                                           nb, na, k0, v0);
     note_launches(1);
     bool first = true;
@@ -570,23 +568,17 @@ cudaError_t spatial_order(const float* pts, long long n, int* order, void* ws, c
     int* hist_scanned = hist + 256 * nblocks + 64;
     int* scan_ws = hist_scanned + 256 * nblocks + 64;
     bounds_init_kernel<<<1, 32, 0, stream>>>(bounds); note_launches(1);
-    long long b = (n + 255) / 256;
-    b = b > 152 * 8 ? 152 * 8 : b;
-    points_bounds_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, bounds); note_launches(1);
+    const unsigned b = capped_blocks(n, 256, 8);
+    points_bounds_kernel<<<b, 256, 0, stream>>>(pts, n, bounds); note_launches(1);
     bounds_decode_kernel<<<1, 32, 0, stream>>>(bounds); note_launches(1);
-    morton_kernel<<<(unsigned)b, 256, 0, stream>>>(pts, n, bounds, k0, v0); note_launches(1);
+    morton_kernel<<<b, 256, 0, stream>>>(pts, n, bounds, k0, v0); note_launches(1);
     bool first = true;
     cudaError_t e = radix_sort_pairs(k0, v0, k1, v1, n, 1 << 30, hist, hist_scanned, scan_ws, &first, stream);
     if (e != cudaSuccess) return e;
     return cudaMemcpyAsync(order, first ? v0 : v1, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, stream);
 }
 
-static unsigned grid_blocks(long long n, int threads) {
-    long long b = (n + threads - 1) / threads;
-    if (b < 1) b = 1;
-    if (b > 152 * 32) b = 152 * 32;
-    return (unsigned)b;
-}
+static unsigned grid_blocks(long long n, int threads) { return capped_blocks(n, threads, 32); }
 
 // --------------------------------------------------------------- phases
 size_t grid_count_workspace_bytes(long long n_tris) {

@@ -65,6 +65,13 @@ struct StageParams {
     int* snk_visible;              // [n_snk] visible sources per sink (may be nullptr)
 };
 
+// Streaming multiprocessors of the current device, queried once per device and
+// cached (the count of a device never changes); 1 if the query fails.
+int device_sm_count();
+// Blocks of `threads` threads covering n items of a grid-stride loop, at least
+// one and at most per_sm blocks per SM of the current device.
+unsigned capped_blocks(long long n, int threads, int per_sm);
+
 // Records the CUDA error that lyem_last_cuda_error() reports (lyem_capi.cu).
 void record_cuda_error(cudaError_t e);
 
@@ -80,6 +87,8 @@ cudaError_t launch_pair_stage(const StageParams& p, int cull, cudaStream_t strea
 cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, long long n_snk, float* out,
                                    int accumulate, cudaStream_t stream);
 int stage_block_threads();
+// Sources per thread block of a pair stage when the caller passes 0 (lyem_capi.cu).
+int auto_src_chunk(long long n_src, long long n_snk, bool grid);
 int brute_max_src_chunk();
 int grid_max_src_chunk();
 

@@ -15,9 +15,6 @@
 // race on the array.
 #include <cuda_runtime.h>
 
-#include <algorithm>
-#include <mutex>
-
 #include "lyem.h"
 #include "lyem_internal.cuh"
 
@@ -26,27 +23,35 @@ namespace {
 constexpr size_t kNoallocScratchBytes = size_t(32) << 20;  // 32 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_address[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device.  In host code the
-// array's name stands for a host-side shadow, so the address is looked up once
-// per device (with that device current) and cached.
+// Device address of g_noalloc_scratch in the current device's context.  In host
+// code the array's name stands for a host-side shadow, not a device address,
+// so the address is looked up with that device current.  It is looked up on
+// every call rather than cached: a cached address would go stale once the
+// caller resets the device (cudaDeviceReset) and the module is loaded again.
 int scratch_address(void** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return LYEM_ERR_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return LYEM_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_address[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return LYEM_ERR_CUDA;
-        g_scratch_address[dev] = p;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        lyem::record_cuda_error(e);
+        return LYEM_ERR_CUDA;
     }
-    *out = g_scratch_address[dev];
+    *out = p;
     return LYEM_OK;
+}
+
+// Source chunk for the fixed scratch: the caller's chunk, else the automatic
+// one when its partial sums fit, else the smallest larger chunk whose partial
+// sums fit; 0 when even the largest chunk's do not.
+int32_t noalloc_chunk(int64_t n_src, int64_t n_snk, bool use_grid, int32_t src_chunk) {
+    const int32_t cap = use_grid ? lyem::grid_max_src_chunk() : lyem::brute_max_src_chunk();
+    if (src_chunk > 0) return src_chunk < cap ? src_chunk : cap;
+    const int32_t automatic = lyem::auto_src_chunk(n_src, n_snk, use_grid);
+    // lyem_pair_stage's workspace: ceil(n_src / chunk) * n_snk * 24 bytes + 256
+    const long long max_chunks = (long long)((kNoallocScratchBytes - 256) / (24ull * (unsigned long long)n_snk));
+    if (max_chunks < 1) return 0;
+    const long long need = (n_src + max_chunks - 1) / max_chunks;
+    const long long chunk = need > automatic ? need : automatic;
+    return chunk <= cap ? (int32_t)chunk : 0;
 }
 
 }  // namespace
@@ -67,25 +72,13 @@ LYEM_API int lyem_pair_stage_noalloc(const float* d_src_pos, const float* d_src_
                                      const int32_t* d_snk_order, int32_t src_chunk, int32_t traversal,
                                      void* stream) {
     if (n_src < 0 || n_snk < 0) return LYEM_ERR_INVALID;
-    const int32_t use_grid = d_cell_start != nullptr;
-    // With an automatic chunk, use the smallest chunk (at least the automatic
-    // one) whose partial sums fit the fixed scratch.
+    const bool use_grid = d_cell_start != nullptr;
     int32_t chunk = src_chunk;
-    if (chunk <= 0 && n_src > 0 && n_snk > 0) {
-        const int32_t cap = use_grid ? lyem::grid_max_src_chunk() : lyem::brute_max_src_chunk();
-        for (int32_t c = 1; c <= cap; ++c) {
-            if (lyem_pair_stage_workspace(n_src, n_snk, n_tris, use_grid, c) <=
-                    lyem_pair_stage_workspace(n_src, n_snk, n_tris, use_grid, 0) &&
-                lyem_pair_stage_workspace(n_src, n_snk, n_tris, use_grid, c) <= kNoallocScratchBytes) {
-                chunk = c;
-                break;
-            }
-        }
-        if (chunk <= 0) chunk = cap;  // too large for the scratch: rejected below
+    if (n_src > 0 && n_snk > 0) {
+        chunk = noalloc_chunk(n_src, n_snk, use_grid, src_chunk);
+        if (chunk <= 0 || lyem_pair_stage_workspace(n_src, n_snk, n_tris, use_grid, chunk) > kNoallocScratchBytes)
+            return LYEM_ERR_WORKSPACE;
     }
-    if (n_src > 0 && n_snk > 0 &&
-        lyem_pair_stage_workspace(n_src, n_snk, n_tris, use_grid, chunk) > kNoallocScratchBytes)
-        return LYEM_ERR_WORKSPACE;
     void* scratch = nullptr;
     int st = scratch_address(&scratch);
     if (st != LYEM_OK) return st;

@@ -269,10 +269,7 @@ __global__ void path_time_kernel(const PathParams p, double* amp, double* arriva
     }
 }
 
-unsigned grid_for(long long n) {
-    long long b = (n + 255) / 256;
-    return (unsigned)(b < 1 ? 1 : (b > 152LL * 16 ? 152LL * 16 : b));
-}
+unsigned grid_for(long long n) { return capped_blocks(n, 256, 16); }
 
 }  // namespace
 }  // namespace lyem

@@ -81,6 +81,28 @@ cudaError_t fma_probe(long long iters, double* fma_per_s, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+int device_sm_count() {
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < kMaxDev) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) return 1;
+    if (dev >= 0 && dev < kMaxDev) cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
+unsigned capped_blocks(long long n, int threads, int per_sm) {
+    long long b = (n + threads - 1) / threads;
+    const long long cap = (long long)device_sm_count() * per_sm;
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
 unsigned int* device_error_word() {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
@@ -494,9 +516,8 @@ cudaError_t launch_reduce_partials(const float* partial, long long n_chunks, lon
                                    int accumulate, cudaStream_t stream) {
     const long long n_elem = 6 * n_snk;
     if (n_elem == 0) return cudaSuccess;
-    long long blocks = (n_elem + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    reduce_partials_kernel<<<(unsigned)blocks, 256, 0, stream>>>(partial, n_chunks, n_elem, out, accumulate); note_launches(1);
+    const unsigned blocks = capped_blocks(n_elem, 256, 16);
+    reduce_partials_kernel<<<blocks, 256, 0, stream>>>(partial, n_chunks, n_elem, out, accumulate); note_launches(1);
     return cudaGetLastError();
 }
 

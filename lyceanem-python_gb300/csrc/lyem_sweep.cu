@@ -196,10 +196,7 @@ cublasHandle_t cublas_for_current_device(cudaStream_t stream, int* err) {
     return g_cublas[dev];
 }
 
-unsigned sweep_blocks(long long n) {
-    long long b = (n + 255) / 256;
-    return (unsigned)(b < 1 ? 1 : (b > 152 * 32 ? 152 * 32 : b));
-}
+unsigned sweep_blocks(long long n) { return capped_blocks(n, 256, 32); }
 }  // namespace
 
 }  // namespace lyem

@@ -130,6 +130,11 @@ CACHE_SIZE = 4
 cache_stats = {"hits": 0, "misses": 0}
 
 
+def clear_cache():
+    """Drops every cached structure (the next model call uploads and grids its solid again)."""
+    _CACHE.clear()
+
+
 def cached_structure(verts, faces, grid_cell=None):
     """Tile_acceleration_structure of (verts, faces) from the scene cache, built on a miss."""
     v = np.ascontiguousarray(verts, dtype=np.float32)

@@ -418,3 +418,38 @@ def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_sa
         if k > 0:
             out[pair[r, 0], pair[r, 1], t0[r]:t0[r] + k] += exc[:k, None] * amp[r][None]
     return out, wake
+
+
+def edge_pairs(src, snk, pairs, tris12, cull=True, eps=EPSILON, rel=1e-5):
+    """For each (n, m) of `pairs` (int (K,2)): True when the segment src[n] -> snk[m] is an epsilon-edge
+    case, i.e. some triangle's Moller-Trumbore test, evaluated in FP64, lies within `rel` of one of the
+    decision thresholds of hit() (lyceanem/src/raycasting.cuh:19-68: determinant against eps, U in
+    [0, 1], V >= 0, U + V <= 1, t inside (2 eps, len - 2 eps)) while every other threshold is met to within
+    the same margin, so that FP32 rounding could decide the pair either way.  Slacks are relative: the
+    determinant's to max(|A|, eps), U, V and U + V as they are, t's to the segment length."""
+    t = np.asarray(tris12, dtype=np.float64).reshape(-1, 12)
+    v0, e1, e2 = t[:, 0:3], t[:, 4:7], t[:, 8:11]
+    src = np.asarray(src, dtype=np.float32).reshape(-1, 3)
+    snk = np.asarray(snk, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros(len(pairs), dtype=bool)
+    for i, (n, m) in enumerate(np.asarray(pairs, dtype=np.int64).reshape(-1, 2)):
+        o = src[n].astype(np.float64)
+        r = snk[m].astype(np.float64) - o
+        length = np.sqrt(r @ r)
+        d = r / length
+        p = np.cross(d, e2)
+        A = np.einsum("ij,ij->i", e1, p)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            tv = o - v0
+            U = np.einsum("ij,ij->i", tv, p) / A
+            q = np.cross(tv, e1)
+            V = (q @ d) / A
+            T = np.einsum("ij,ij->i", e2, q) / A
+            det = ((A if cull else np.abs(A)) - eps) / np.maximum(np.abs(A), eps)
+            slack = np.stack([det, U, 1.0 - U, V, 1.0 - U - V, (T - 2 * eps) / length,
+                              (length - 2 * eps - T) / length], 1)
+        slack = np.nan_to_num(slack, nan=-np.inf)
+        near = (np.abs(slack) < rel).any(1) & (slack > -rel).all(1)
+        out[i] = bool(near.any())
+    return out
+

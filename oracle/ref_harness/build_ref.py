@@ -1,6 +1,7 @@
 """Compiles harness.cu against the reference's headers into oracle/_ref/ (test infrastructure only).
 
-Run where the reference tree is mounted (default /root/reference).  Builds two
+Run where the reference tree is mounted: its root is the argument, else the
+environment variable LYEM_REFERENCE_ROOT, else /root/reference.  Builds two
 cubins for sm_103a with the reference's release flags (-O3 -DNDEBUG): the
 default (nvcc free to contract a*b+c into FMA, as the reference's own build)
 and --fmad=false, which bracket the reference binary's arithmetic.
@@ -14,8 +15,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 
 
-def build(ref_root="/root/reference", verbose=False):
-    src = os.path.join(ref_root, "lyceanem", "src")
+DEFAULT_ROOT = "/root/reference"
+
+
+def reference_root():
+    """Root of the mounted reference tree (LYEM_REFERENCE_ROOT overrides the default)."""
+    return os.environ.get("LYEM_REFERENCE_ROOT", DEFAULT_ROOT)
+
+
+def build(ref_root=None, verbose=False):
+    """Builds the harness cubins; None when the reference's sources are not mounted."""
+    src = os.path.join(ref_root or reference_root(), "lyceanem", "src")
     if not os.path.isdir(src):
         return None
     import pybind11

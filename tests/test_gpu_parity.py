@@ -249,6 +249,41 @@ def test_bounce_scene_reduced_vs_oracle():
         assert np.array_equal(r.mask().cpu().numpy(), og.mask(a, b))
 
 
+def test_bounce_config_full_geometry_slice():
+    """The 28 GHz one-bounce workload at full geometry (32x32 array, all 120,000 triangles, the 0.5 m
+    grid) on a slice of its sinks (every 128th, 511) and scatter points (every 125th, 400), through the
+    same kernels, processing orders and grid as the benchmarked step: per-stage masks bit-exact against
+    the oracle, the sink field within FIELD_TOL of the FP64 oracle."""
+    from lyceanem_gb300 import scenes
+    P = _P()
+    s = scenes.bounce_scene()
+    beta = 2 * np.pi / s.wavelength
+    snk, snk_n = s.snk[::128], s.snk_n[::128]
+    scat, scat_n = s.scat[::125], s.scat_n[::125]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    tris = P.pack_triangles(t(s.verts), t(s.faces))
+    grid = P.UniformGrid(tris, cell=s.cell)
+    src, E, yk, ykn, pk, pkn = t(s.src), t(s.E), t(snk), t(snk_n), t(scat), t(scat_n)
+    o_snk, o_scat = P.direction_order(yk, grid.centre), P.spatial_order(pk)
+    r0 = P.pair_stage(src, E, yk, ykn, beta=beta, grid=grid, want_mask=True, snk_order=o_snk)
+    r1 = P.pair_stage(src, E, pk, pkn, beta=beta, grid=grid, want_mask=True, snk_order=o_scat)
+    field = r0.sink.clone()
+    r2 = P.pair_stage(pk, r1.sink, yk, ykn, beta=beta, grid=grid, src_W=r1.sink, sink_out=field, accumulate=True,
+                      want_mask=True, src_order=o_scat, snk_order=o_snk)
+    _no_device_errors()
+    og = O.Grid(O.pack_triangles(s.verts, s.faces), s.cell)
+    m0, m1, m2 = og.mask(s.src, snk), og.mask(s.src, scat), og.mask(scat, snk)
+    assert np.array_equal(r0.mask().cpu().numpy(), m0)
+    assert np.array_equal(r1.mask().cpu().numpy(), m1)
+    assert np.array_equal(r2.mask().cpu().numpy(), m2)
+    assert 0 < m2.sum() < m2.size and 0 < m0.sum() < m0.size  # the slice sees both blocked and visible paths
+    ep = O.sink_field(s.src, s.E, scat, scat_n, 0.0, beta, mask=m1)
+    ref = O.sink_field(s.src, s.E, snk, snk_n, 0.0, beta, mask=m0)
+    ref = ref + O.sink_field(scat, ep, snk, snk_n, 0.0, beta, srcW=ep, mask=m2)
+    assert rel_err(r1.sink.cpu().numpy(), ep) < FIELD_TOL
+    assert rel_err(field.cpu().numpy(), ref) < FIELD_TOL
+
+
 def test_em_dropin_functions():
     """The four lyceanem.em functions against the oracle network."""
     from lyceanem_gb300 import em
