@@ -44,6 +44,17 @@ PARITY_STRIDE = 16
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic.json")
 
 
+def measured_peak(key):
+    """A peak of MEASURED_PEAKS.json (TFLOP/s or GB/s) and where it came from; the profiling recipe's
+    fallback when the file is absent."""
+    fallback = {"bf16_tflops": 1900.0, "hbm_gbs": 6800.0}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key]), f"measured ({key} of MEASURED_PEAKS.json)"
+    except (OSError, ValueError, KeyError):
+        return fallback[key], "fallback (no measured peak file)"
+
+
 def traffic_record(workload):
     """The recorded DRAM traffic of the dominant kernel of `workload` (dict with bytes, kernel, command,
     commit) or None."""
@@ -380,8 +391,16 @@ def run_sweep(args, n_check=256, reps=5):
     flops = 8.0 * M * N * K * 3
     res = {"n_elements": N, "n_sinks": M, "n_beams": K, "network_form_ms": form_ms,
            "algorithmic_flops": flops}
+    # tensor work the kernel issues: 3 components x 3 real products x 3 split products of 2 flops per
+    # MAC over whole tiles (128 sinks x 256 beams x 64 sources)
+    rnd = lambda a, b: -(-a // b) * b  # noqa: E731
+    issued = 3 * 9 * 2.0 * rnd(M, 128) * rnd(K, 256) * rnd(N, 64)
+    peak, peak_src = measured_peak("bf16_tflops")
+    res["tensor_issued_flops"] = issued
     outs = {}
-    for mode in ("fp32", "bf16x3", "fp16x3", "bf16x3g", "fp16x3g"):
+    for name, mode, k_tile in (("fp32", "fp32", 64), ("bf16x3g", "bf16x3g", 64), ("fp16x3g", "fp16x3g", 64),
+                               ("bf16x3g_k32", "bf16x3g", 32)):
+        BS.set_k_tile(k_tile)
         sw = BS.BeamSweep(G, mode)
         out = sw.run(W)
         torch.cuda.synchronize()
@@ -394,10 +413,22 @@ def run_sweep(args, n_check=256, reps=5):
             ev.append((x, y))
         torch.cuda.synchronize()
         ms = min(x.elapsed_time(y) for x, y in ev)
-        outs[mode] = sw.fields(out)[torch.from_numpy(pick).cuda()].cpu().numpy()
-        res[mode] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12}
+        outs[name] = sw.fields(out)[torch.from_numpy(pick).cuda()].cpu().numpy()
+        res[name] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12}
+        if mode != "fp32":
+            res[name]["k_tile"] = k_tile
+            res[name]["tensor_tflops_issued"] = issued / (ms * 1e-3) / 1e12
+            res[name]["tensor_frac"] = issued / (ms * 1e-3) / 1e12 / peak
         del sw, out
         torch.cuda.empty_cache()
+    BS.set_k_tile(64)
+    st, flags = P.device_errors()
+    res["device_errors"] = [int(st), int(flags)]
+    res["roofline"] = {"bound": "tensor", "kernel": "sweep_tc_kernel (bf16x3g, k-tile 64)",
+                       "achieved": res["bf16x3g"]["tensor_tflops_issued"], "peak": peak, "unit": "TFLOP/s",
+                       "frac": res["bf16x3g"]["tensor_frac"], "peak_source": peak_src,
+                       "note": "achieved = issued tensor flops (whole tiles, 9 real products per complex product) / "
+                               "time of one run (weight split + the three component products)"}
     del G
     # FP64 reference on the sampled sinks: oracle visibility + FP64 network, FP64 product
     og = O.Grid(O.pack_triangles(s.verts, s.faces), s.cell)
@@ -407,8 +438,6 @@ def run_sweep(args, n_check=256, reps=5):
     E64 = np.einsum("nmc,kn->mkc", G64, s.weights.astype(np.complex128), optimize=True)
     for mode, E in outs.items():
         res[mode]["rel_err_fp64"] = float(np.linalg.norm(E - E64) / np.linalg.norm(E64))
-    res["speedup_bf16x3_vs_fp32"] = res["fp32"]["ms"] / res["bf16x3"]["ms"]
-    res["speedup_fp16x3_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3"]["ms"]
     res["speedup_bf16x3g_vs_fp32"] = res["fp32"]["ms"] / res["bf16x3g"]["ms"]
     res["speedup_fp16x3g_vs_fp32"] = res["fp32"]["ms"] / res["fp16x3g"]["ms"]
     res["error_sample"] = f"{n_check} seeded sinks x {K} beams x 3 components, relative Frobenius norm"

@@ -224,13 +224,22 @@ LYEM_API int lyem_mask_to_bytes(const uint32_t *d_mask_bits, int64_t n_src, int6
  * Replaces re-running the whole model once per excitation
  * (lyceanem/models/frequency_domain.py:858-921, multiE) and the host GEMMs of
  * lyceanem/models/frequency_domain.py:258-260.
- * mode 0: plain complex64 FP32 (cublasCgemm); 1: BF16 split (x = hi + lo,
- * hi*hi + hi*lo + lo*hi on the tensor cores, FP32 accumulation); 2: FP16 split.
+ * mode 0: plain complex64 FP32 (cublasCgemm), the comparison path.
+ * mode 3: BF16 split on the tensor cores (this library's tcgen05 kernel): each
+ *   real operand x = hi + lo, the complex product from three real products
+ *   (Gauss: Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi); 6 M N K flops per component
+ *   instead of 8), each accumulated in FP32 as hi*hi + lo*hi + hi*lo.
+ * mode 4: the same with FP16 halves; the network (per component) and the
+ *   weights are scaled by powers of two that put their largest magnitude at
+ *   2^14 (no overflow, few subnormal halves) and the result is unscaled exactly.
+ * Modes 1 and 2 (the four-product forms of earlier versions) are refused with
+ * LYEM_ERR_INVALID.
  * Step 1 converts G into the GEMM operand (d_network, lyem_sweep_network_bytes;
- * ld >= n_snk, a multiple of 8); step 2 converts W (split modes only, d_B,
- * lyem_sweep_weights_bytes); step 3 runs the three component GEMMs into d_out,
- * complex64 [3][n_beams][ldc] (component c, beam k: column-major E[:, k, c];
- * ldc >= ld, rows n_snk..ld-1 receive zeros). */
+ * ld >= n_snk, a multiple of 8; modes 3, 4: 256-byte aligned); step 2 converts
+ * W (modes 3, 4 only, d_B, lyem_sweep_weights_bytes, 256-byte aligned); step 3
+ * runs the three component products into d_out, complex64 [3][n_beams][ldc]
+ * (component c, beam k: column-major E[:, k, c]; ldc >= ld; mode 0 writes
+ * zeros to rows n_snk..ld-1, modes 3, 4 leave them untouched). */
 LYEM_API size_t lyem_sweep_network_bytes(int64_t n_src, int64_t ld, int32_t mode);
 LYEM_API size_t lyem_sweep_weights_bytes(int64_t n_src, int64_t n_beams, int32_t mode);
 LYEM_API int lyem_sweep_prepare_network(const float *d_pairs, int64_t n_src, int64_t n_snk, int32_t mode, int64_t ld,
@@ -239,14 +248,17 @@ LYEM_API int lyem_sweep_prepare_weights(const float *d_W, int64_t n_src, int64_t
                                         void *stream);
 LYEM_API int lyem_sweep_run(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
                             const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *stream);
-/* Modes 3 (BF16) and 4 (FP16): the same split with the complex product in three
- * real products (Gauss: Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi)), 6 M N K flops per
- * component instead of 8; they need a scratch of lyem_sweep_workspace_bytes
- * (three FP32 ld x n_beams products) and lyem_sweep_run_ws (any mode). */
+/* lyem_sweep_run with a workspace argument, kept for callers of earlier
+ * versions: no mode needs a workspace now (lyem_sweep_workspace_bytes returns
+ * 0) and d_ws / ws_bytes are ignored. */
 LYEM_API size_t lyem_sweep_workspace_bytes(int64_t ld, int64_t n_beams, int32_t mode);
 LYEM_API int lyem_sweep_run_ws(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
                                const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *d_ws,
                                size_t ws_bytes, void *stream);
+/* Sources per pipeline stage of the tensor-core kernel (process-wide): 64
+ * (default; 128-byte swizzled rows, 2 stages) or 32 (64-byte rows, 4 stages).
+ * Results are the same; only the speed differs.  No counterpart in the reference. */
+LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile);
 
 /* --------------------------------------------------------------- adjoint */
 

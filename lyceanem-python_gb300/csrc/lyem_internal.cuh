@@ -92,6 +92,14 @@ int auto_src_chunk(long long n_src, long long n_snk, bool grid);
 int brute_max_src_chunk();
 int grid_max_src_chunk();
 
+// Beam sweep on the tensor cores (lyem_sweep_tc.cu).  Operand buffers start
+// with a header of kSweepHeaderBytes holding the power-of-two scales (floats
+// [0, 3) of the network, float 0 of the weights) ahead of the K-major planes.
+constexpr size_t kSweepHeaderBytes = 256;
+extern int sweep_tc_k_tile;  // sources per pipeline stage: 64 (128-byte rows) or 32 (64-byte rows)
+int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int64_t n_snk, int64_t ld,
+                    int64_t n_beams, bool bf16, float* out, int64_t ldc, cudaStream_t stream);
+
 // Grid build (lyem_grid.cu).
 cudaError_t launch_tris_bounds(const float4* tris, long long n_tris, float* bounds6, cudaStream_t stream);
 

@@ -9,25 +9,17 @@
 // (lyceanem/models/frequency_domain.py:258-260).
 //
 // Modes:
-//   0  plain complex64 FP32: cublasCgemm on the complex matrices;
-//   1  BF16 split: x = hi + lo with hi = bf16(x), lo = bf16(x - hi); the
-//      product is hi*hi + hi*lo + lo*hi on the tensor cores with FP32
-//      accumulation (lo*lo, ~2^-16 relative, is dropped);
-//   2  FP16 split, same scheme with binary16 (11 + 11 significant bits).
-//   3, 4  BF16 / FP16 split with the complex product in three real products
-//      (Gauss): with G = Gr + j Gi and W = Wr + j Wi,
-//        T1 = Gr Wr,  T2 = Gi Wi,  T3 = (Gr + Gi)(Wr + Wi),
-//        Re E = T1 - T2,  Im E = T3 - T1 - T2,
-//      each T a real (M x N)(N x K) GEMM of split operands (6 M N K flops per
-//      component against 8 M N K), the sums Gr + Gi and Wr + Wi formed in FP32
-//      before the split.  The three split products of one T run as two GEMMs:
-//      [hi | lo] (M x 2N) times [hi ; hi] (2N x K), then hi times lo.
-// For the split modes 1, 2 the complex product is one real GEMM in interleaved form:
-//   A' = [G | jG] as a (2M x 2N) real column-major matrix (column n holds the
-//   interleaved (re, im) of G[:, n]; column N + n holds j G[:, n] = (-im, re)),
-//   B' = [Re W^T ; Im W^T] (2N x K),
-// so C' = A' B' is (2M x K) real and, read as complex64 (M x K) column-major,
-// is exactly E[:, :, c] in the layout cublasCgemm writes.
+//   0  plain complex64 FP32 (cublasCgemm), the comparison path;
+//   3  BF16 split on the tensor cores: each real operand x = hi + lo with
+//      hi = bf16(x), lo = bf16(x - hi); the complex product from three real
+//      products (Gauss: Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi)), each as
+//      hi*hi + lo*hi + hi*lo with FP32 accumulation (lyem_sweep_tc.cu);
+//   4  the same with FP16 halves, after a power-of-two scaling of the network
+//      (per component) and of the weights that puts their largest magnitude at
+//      2^14, so that no half overflows and few are subnormal.
+// Modes 3 and 4 read K-major operand planes written here (sources contiguous):
+// a 256-byte header (the scales) followed by 18 network planes [ld][kpad] or 6
+// weight planes [n_beams][kpad], kpad = n_src rounded up to a multiple of 8.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -53,96 +45,122 @@ __device__ __forceinline__ float from_lp<__nv_bfloat16>(__nv_bfloat16 x) { retur
 template <>
 __device__ __forceinline__ float from_lp<__half>(__half x) { return __half2float(x); }
 
-// Network [N][M][3] complex64 -> per component A' hi/lo planes, each
-// (2 ld x 2N) column-major; rows past 2M are zero padding.
-template <typename T>
-__global__ void split_network_kernel(const float2* __restrict__ pairs, long long N, long long M, long long ld,
-                                     float scale, T* __restrict__ out) {
-    const long long plane = 2 * ld * 2 * N;  // elements of one (hi or lo) plane
-    const long long total = N * ld;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+// Largest |Gr|, |Gi|, |Gr + Gi| per component of the network [N][M][3]
+// (max_bits[c], float bits: non-negative floats order as their bit patterns).
+__global__ void network_maxabs_kernel(const float2* __restrict__ pairs, long long n_pairs,
+                                      unsigned int* __restrict__ max_bits) {
+    float mx[3] = {0.f, 0.f, 0.f};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_pairs;
          i += (long long)gridDim.x * blockDim.x) {
-        const long long n = i / ld, m = i - n * ld;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            float2 g = m < M ? pairs[(n * M + m) * 3 + c] : make_float2(0.f, 0.f);
-            g.x *= scale;
-            g.y *= scale;
-            const T hr = to_lp<T>(g.x), hi_ = to_lp<T>(g.y);
-            const T lr = to_lp<T>(g.x - from_lp<T>(hr)), li = to_lp<T>(g.y - from_lp<T>(hi_));
-            T* hp = out + (long long)(2 * c) * plane;
-            T* lp = hp + plane;
-            const long long col = 2 * ld * n, colj = 2 * ld * (N + n);
-            hp[col + 2 * m] = hr;
-            hp[col + 2 * m + 1] = hi_;
-            lp[col + 2 * m] = lr;
-            lp[col + 2 * m + 1] = li;
-            // j G = (-im, re)
-            hp[colj + 2 * m] = to_lp<T>(-from_lp<T>(hi_));
-            hp[colj + 2 * m + 1] = hr;
-            lp[colj + 2 * m] = to_lp<T>(-from_lp<T>(li));
-            lp[colj + 2 * m + 1] = lr;
+            const float2 g = pairs[3 * i + c];
+            mx[c] = fmaxf(mx[c], fmaxf(fmaxf(fabsf(g.x), fabsf(g.y)), fabsf(__fadd_rn(g.x, g.y))));
         }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float v = mx[c];
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if ((threadIdx.x & 31) == 0 && v > 0.f) atomicMax(max_bits + c, __float_as_uint(v));
     }
 }
 
-// Network [N][M][3] -> per component six planes (ld x N, column-major, rows
-// past M zero): Gr hi, Gr lo, Gi hi, Gi lo, Gs hi, Gs lo (Gs = Gr + Gi), so that
-// each part's hi and lo planes form one (ld x 2N) matrix.
-template <typename T>
-__global__ void split_network_gauss_kernel(const float2* __restrict__ pairs, long long N, long long M, long long ld,
-                                           T* __restrict__ out) {
-    const long long plane = ld * N;
-    const long long total = N * ld;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long n = i / ld, m = i - n * ld;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float2 g = m < M ? pairs[(n * M + m) * 3 + c] : make_float2(0.f, 0.f);
-            const float part[3] = {g.x, g.y, __fadd_rn(g.x, g.y)};
-            T* base = out + (long long)(6 * c) * plane;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const T h = to_lp<T>(part[q]);
-                base[(2 * q) * plane + i] = h;
-                base[(2 * q + 1) * plane + i] = to_lp<T>(part[q] - from_lp<T>(h));
-            }
-        }
-    }
-}
-
-// Weights W [K][N] -> per part (r, i, s = r + i) a (2N x K) column-major
-// [hi ; hi] matrix followed by a (N x K) lo matrix.
-template <typename T>
-__global__ void split_weights_gauss_kernel(const float2* __restrict__ W, long long N, long long K, T* __restrict__ out) {
-    const long long part_elems = 3 * N * K;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N * K;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long k = i / N, n = i - k * N;
+// Largest |Wr|, |Wi|, |Wr + Wi| of the weights [K][N] (max_bits[0]).
+__global__ void weights_maxabs_kernel(const float2* __restrict__ W, long long n, unsigned int* __restrict__ max_bits) {
+    float mx = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 w = W[i];
-        const float part[3] = {w.x, w.y, __fadd_rn(w.x, w.y)};
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(w.x), fabsf(w.y)), fabsf(__fadd_rn(w.x, w.y))));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(max_bits, __float_as_uint(mx));
+}
+
+// Header floats [0, n): the scales 2^(14 - e) with max < 2^e (FP16), or 1 (BF16).
+__global__ void sweep_scales_kernel(float* __restrict__ hdr, int n, int unit) {
+    const int i = threadIdx.x;
+    if (i >= n) return;
+    const float mx = __uint_as_float(reinterpret_cast<const unsigned int*>(hdr)[4 + i]);
+    float s = 1.f;
+    if (!unit && mx > 0.f && isfinite(mx)) {
+        int e = 0;
+        frexpf(mx, &e);  // mx = f 2^e, 0.5 <= f < 1
+        s = ldexpf(1.f, 14 - e);
+    }
+    hdr[i] = s;
+}
+
+// hi and lo halves of x (already scaled) as 16-bit bit patterns.
+template <typename T>
+__device__ __forceinline__ void split16(float x, unsigned short& hi, unsigned short& lo) {
+    const T h = to_lp<T>(x);
+    const T l = to_lp<T>(__fsub_rn(x, from_lp<T>(h)));
+    hi = *reinterpret_cast<const unsigned short*>(&h);
+    lo = *reinterpret_cast<const unsigned short*>(&l);
+}
+
+// Network [N][M][3] complex64 -> 18 K-major planes [ld][kpad] (plane (3 c + q) 2 + h for component c,
+// part q in (r, i, s = r + i), half h), scaled by hdr[c].  A block transposes a tile of 32 sinks x 32
+// sources through shared memory: loads run along the sinks, stores along the sources.
+template <typename T>
+__global__ void __launch_bounds__(256) split_network_kmajor_kernel(const float2* __restrict__ pairs, long long N,
+                                                                   long long M, long long ld, long long kpad,
+                                                                   const float* __restrict__ hdr,
+                                                                   unsigned short* __restrict__ planes) {
+    __shared__ float2 tile[3][32][33];
+    const long long m0 = (long long)blockIdx.x * 32, n0 = (long long)blockIdx.y * 32;
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int r = 0; r < 12; ++r) {  // 32 sources x 96 (sink, component) floats2, contiguous per source
+        const int i = tid + 256 * r;
+        const int n = i / 96, j = i - n * 96, m = j / 3, c = j - m * 3;
+        float2 g = make_float2(0.f, 0.f);
+        if (n0 + n < N && m0 + m < M) g = pairs[((n0 + n) * M + m0) * 3 + j];
+        tile[c][n][m] = g;
+    }
+    __syncthreads();
+    const float sc[3] = {hdr[0], hdr[1], hdr[2]};
+    const long long plane = ld * kpad;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {  // 3 components x 32 sinks x 16 source pairs
+        const int i = tid + 256 * r;
+        const int np = i & 15, m = (i >> 4) & 31, c = i >> 9;
+        const long long row = m0 + m, col = n0 + 2 * np;
+        if (row >= ld || col >= kpad) continue;
+        const float2 g0 = tile[c][2 * np][m], g1 = tile[c][2 * np + 1][m];
+        const float p0[3] = {g0.x * sc[c], g0.y * sc[c], __fadd_rn(g0.x, g0.y) * sc[c]};
+        const float p1[3] = {g1.x * sc[c], g1.y * sc[c], __fadd_rn(g1.x, g1.y) * sc[c]};
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            T* dup = out + q * part_elems;
-            T* lo = dup + 2 * N * K;
-            const T h = to_lp<T>(part[q]);
-            dup[k * 2 * N + n] = h;
-            dup[k * 2 * N + N + n] = h;
-            lo[k * N + n] = to_lp<T>(part[q] - from_lp<T>(h));
+            unsigned short h0, l0, h1, l1;
+            split16<T>(p0[q], h0, l0);
+            split16<T>(p1[q], h1, l1);
+            unsigned short* hp = planes + (long long)((c * 3 + q) * 2) * plane + row * kpad + col;
+            *reinterpret_cast<unsigned int*>(hp) = (unsigned int)h0 | ((unsigned int)h1 << 16);
+            *reinterpret_cast<unsigned int*>(hp + plane) = (unsigned int)l0 | ((unsigned int)l1 << 16);
         }
     }
 }
 
-// out (complex64, column-major ld x K with leading dimension ldc) from the three
-// real products T1, T2, T3 (ld x K each, consecutive in t).
-__global__ void gauss_combine_kernel(const float* __restrict__ t, long long ld, long long K, long long ldc,
-                                     float2* __restrict__ out) {
-    const long long n = ld * K;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float t1 = t[i], t2 = t[n + i], t3 = t[2 * n + i];
-        const long long k = i / ld, m = i - k * ld;
-        out[k * ldc + m] = make_float2(__fsub_rn(t1, t2), __fsub_rn(__fsub_rn(t3, t1), t2));
+// Weights W [K][N] complex64 -> 6 K-major planes [K][kpad] (plane 2 q + h), scaled by hdr[0].
+template <typename T>
+__global__ void split_weights_kmajor_kernel(const float2* __restrict__ W, long long N, long long K, long long kpad,
+                                            const float* __restrict__ hdr, unsigned short* __restrict__ planes) {
+    const float s = hdr[0];
+    const long long plane = K * kpad;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < K * kpad;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long k = i / kpad, n = i - k * kpad;
+        const float2 w = n < N ? W[k * N + n] : make_float2(0.f, 0.f);
+        const float part[3] = {w.x * s, w.y * s, __fadd_rn(w.x, w.y) * s};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            unsigned short h, l;
+            split16<T>(part[q], h, l);
+            planes[(2 * q) * plane + i] = h;
+            planes[(2 * q + 1) * plane + i] = l;
+        }
     }
 }
 
@@ -156,22 +174,6 @@ __global__ void complex_network_kernel(const float2* __restrict__ pairs, long lo
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             out[(long long)c * N * ld + i] = m < M ? pairs[(n * M + m) * 3 + c] : make_float2(0.f, 0.f);
-    }
-}
-
-// Weights W [K][N] complex64 -> B' hi/lo planes (2N x K) column-major.
-template <typename T>
-__global__ void split_weights_kernel(const float2* __restrict__ W, long long N, long long K, T* __restrict__ out) {
-    const long long plane = 2 * N * K;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N * K;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long k = i / N, n = i - k * N;
-        const float2 w = W[i];
-        const T hr = to_lp<T>(w.x), hi_ = to_lp<T>(w.y);
-        out[k * 2 * N + n] = hr;
-        out[k * 2 * N + N + n] = hi_;
-        out[plane + k * 2 * N + n] = to_lp<T>(w.x - from_lp<T>(hr));
-        out[plane + k * 2 * N + N + n] = to_lp<T>(w.y - from_lp<T>(hi_));
     }
 }
 
@@ -205,66 +207,94 @@ using namespace lyem;
 
 extern "C" {
 
+namespace {
+bool split_mode(int32_t mode) { return mode == 3 || mode == 4; }
+bool valid_mode(int32_t mode) { return mode == 0 || split_mode(mode); }
+long long kpad_of(long long n_src) { return (n_src + 7) / 8 * 8; }
+}  // namespace
+
 LYEM_API size_t lyem_sweep_network_bytes(int64_t n_src, int64_t ld, int32_t mode) {
-    if (n_src <= 0 || ld <= 0) return 0;
+    if (n_src <= 0 || ld <= 0 || !valid_mode(mode)) return 0;
     if (mode == 0) return (size_t)3 * n_src * ld * 8;
-    if (mode >= 3) return (size_t)3 * 6 * ld * n_src * 2;
-    return (size_t)3 * 2 * (2 * ld) * (2 * n_src) * 2;
+    return kSweepHeaderBytes + (size_t)18 * ld * kpad_of(n_src) * 2;
 }
 
 LYEM_API size_t lyem_sweep_weights_bytes(int64_t n_src, int64_t n_beams, int32_t mode) {
-    if (n_src <= 0 || n_beams <= 0 || mode == 0) return 0;
-    if (mode >= 3) return (size_t)3 * 3 * n_src * n_beams * 2;
-    return (size_t)2 * (2 * n_src) * n_beams * 2;
+    if (n_src <= 0 || n_beams <= 0 || !split_mode(mode)) return 0;
+    return kSweepHeaderBytes + (size_t)6 * n_beams * kpad_of(n_src) * 2;
 }
 
 LYEM_API size_t lyem_sweep_workspace_bytes(int64_t ld, int64_t n_beams, int32_t mode) {
-    if (ld <= 0 || n_beams <= 0 || mode < 3) return 0;
-    return (size_t)3 * ld * n_beams * 4;
+    (void)ld;
+    (void)n_beams;
+    (void)mode;
+    return 0;  // the tensor-core kernel combines the three products in TMEM
+}
+
+LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile) {
+    if (k_tile != 32 && k_tile != 64) return LYEM_ERR_INVALID;
+    sweep_tc_k_tile = k_tile;
+    return LYEM_OK;
 }
 
 LYEM_API int lyem_sweep_prepare_network(const float* d_pairs, int64_t n_src, int64_t n_snk, int32_t mode, int64_t ld,
                                         void* d_network, void* stream) {
-    if (n_src < 0 || n_snk < 0 || mode < 0 || mode > 4 || ld < n_snk || (ld & 7)) return LYEM_ERR_INVALID;
+    if (n_src < 0 || n_snk < 0 || !valid_mode(mode) || ld < n_snk || (ld & 7)) return LYEM_ERR_INVALID;
     if (n_src == 0 || n_snk == 0) return LYEM_OK;
-    if (!d_pairs || !d_network) return LYEM_ERR_INVALID;
+    if (!d_pairs || !d_network || (reinterpret_cast<uintptr_t>(d_network) & 255)) return LYEM_ERR_INVALID;
+    if (split_mode(mode) && (n_src > 0x7fffffffLL || ld > 0x7fffffffLL)) return LYEM_ERR_OVERFLOW;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const float2* P = reinterpret_cast<const float2*>(d_pairs);
-    const unsigned b = sweep_blocks(n_src * ld);
-    if (mode == 0)
-        complex_network_kernel<<<b, 256, 0, s>>>(P, n_src, n_snk, ld, reinterpret_cast<float2*>(d_network));
-    else if (mode == 1)
-        split_network_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, 1.f,
-                                                             reinterpret_cast<__nv_bfloat16*>(d_network));
-    else if (mode == 3)
-        split_network_gauss_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(P, n_src, n_snk, ld,
-                                                                   reinterpret_cast<__nv_bfloat16*>(d_network));
-    else if (mode == 4)
-        split_network_gauss_kernel<__half><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, reinterpret_cast<__half*>(d_network));
+    if (mode == 0) {
+        complex_network_kernel<<<sweep_blocks(n_src * ld), 256, 0, s>>>(P, n_src, n_snk, ld,
+                                                                      reinterpret_cast<float2*>(d_network));
+        note_launches(1);
+        return cudaGetLastError() == cudaSuccess ? LYEM_OK : LYEM_ERR_CUDA;
+    }
+    float* hdr = static_cast<float*>(d_network);
+    unsigned short* planes = reinterpret_cast<unsigned short*>(static_cast<unsigned char*>(d_network) + kSweepHeaderBytes);
+    if (cudaMemsetAsync(hdr, 0, 32, s) != cudaSuccess) return LYEM_ERR_CUDA;
+    if (mode == 4) {
+        network_maxabs_kernel<<<sweep_blocks(n_src * n_snk), 256, 0, s>>>(P, n_src * n_snk,
+                                                                         reinterpret_cast<unsigned int*>(hdr) + 4);
+        note_launches(1);
+    }
+    sweep_scales_kernel<<<1, 32, 0, s>>>(hdr, 3, mode == 3);
+    const long long kpad = kpad_of(n_src);
+    const dim3 grid((unsigned)((ld + 31) / 32), (unsigned)((kpad + 31) / 32));
+    if (grid.y > 65535u) return LYEM_ERR_OVERFLOW;
+    if (mode == 3)
+        split_network_kmajor_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(P, n_src, n_snk, ld, kpad, hdr, planes);
     else
-        split_network_kernel<__half><<<b, 256, 0, s>>>(P, n_src, n_snk, ld, 1.f, reinterpret_cast<__half*>(d_network));
-    note_launches(1);
+        split_network_kmajor_kernel<__half><<<grid, 256, 0, s>>>(P, n_src, n_snk, ld, kpad, hdr, planes);
+    note_launches(2);
     return cudaGetLastError() == cudaSuccess ? LYEM_OK : LYEM_ERR_CUDA;
 }
 
 LYEM_API int lyem_sweep_prepare_weights(const float* d_W, int64_t n_src, int64_t n_beams, int32_t mode, void* d_B,
                                         void* stream) {
-    if (n_src < 0 || n_beams < 0 || mode < 0 || mode > 4) return LYEM_ERR_INVALID;
+    if (n_src < 0 || n_beams < 0 || !valid_mode(mode)) return LYEM_ERR_INVALID;
     if (mode == 0 || n_src == 0 || n_beams == 0) return LYEM_OK;
-    if (!d_W || !d_B) return LYEM_ERR_INVALID;
+    if (!d_W || !d_B || (reinterpret_cast<uintptr_t>(d_B) & 255)) return LYEM_ERR_INVALID;
+    if (n_src > 0x7fffffffLL || n_beams > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const float2* W = reinterpret_cast<const float2*>(d_W);
-    const unsigned b = sweep_blocks(n_src * n_beams);
-    if (mode == 1)
-        split_weights_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__nv_bfloat16*>(d_B));
-    else if (mode == 2)
-        split_weights_kernel<__half><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__half*>(d_B));
-    else if (mode == 3)
-        split_weights_gauss_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(W, n_src, n_beams,
-                                                                   reinterpret_cast<__nv_bfloat16*>(d_B));
+    float* hdr = static_cast<float*>(d_B);
+    unsigned short* planes = reinterpret_cast<unsigned short*>(static_cast<unsigned char*>(d_B) + kSweepHeaderBytes);
+    if (cudaMemsetAsync(hdr, 0, 32, s) != cudaSuccess) return LYEM_ERR_CUDA;
+    if (mode == 4) {
+        weights_maxabs_kernel<<<sweep_blocks(n_src * n_beams), 256, 0, s>>>(W, n_src * n_beams,
+                                                                           reinterpret_cast<unsigned int*>(hdr) + 4);
+        note_launches(1);
+    }
+    sweep_scales_kernel<<<1, 32, 0, s>>>(hdr, 1, mode == 3);
+    const long long kpad = kpad_of(n_src);
+    const unsigned b = sweep_blocks(n_beams * kpad);
+    if (mode == 3)
+        split_weights_kmajor_kernel<__nv_bfloat16><<<b, 256, 0, s>>>(W, n_src, n_beams, kpad, hdr, planes);
     else
-        split_weights_gauss_kernel<__half><<<b, 256, 0, s>>>(W, n_src, n_beams, reinterpret_cast<__half*>(d_B));
-    note_launches(1);
+        split_weights_kmajor_kernel<__half><<<b, 256, 0, s>>>(W, n_src, n_beams, kpad, hdr, planes);
+    note_launches(2);
     return cudaGetLastError() == cudaSuccess ? LYEM_OK : LYEM_ERR_CUDA;
 }
 
@@ -274,80 +304,38 @@ LYEM_API int lyem_sweep_run_ws(const void* d_network, int64_t n_src, int64_t n_s
 
 LYEM_API int lyem_sweep_run(const void* d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float* d_W,
                             const void* d_B, int64_t n_beams, int32_t mode, float* d_out, int64_t ldc, void* stream) {
-    if (mode > 2) return LYEM_ERR_INVALID;  // the three-product modes need lyem_sweep_run_ws
     return lyem_sweep_run_ws(d_network, n_src, n_snk, ld, d_W, d_B, n_beams, mode, d_out, ldc, nullptr, 0, stream);
 }
 
 LYEM_API int lyem_sweep_run_ws(const void* d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float* d_W,
                                const void* d_B, int64_t n_beams, int32_t mode, float* d_out, int64_t ldc, void* d_ws,
                                size_t ws_bytes, void* stream) {
-    if (n_src <= 0 || n_snk <= 0 || n_beams <= 0 || mode < 0 || mode > 4 || ld < n_snk || ldc < ld)
+    (void)d_ws;
+    (void)ws_bytes;
+    if (n_src <= 0 || n_snk <= 0 || n_beams <= 0 || !valid_mode(mode) || ld < n_snk || ldc < ld)
         return LYEM_ERR_INVALID;
-    if (mode >= 3 && (!d_ws || ws_bytes < lyem_sweep_workspace_bytes(ld, n_beams, mode))) return LYEM_ERR_WORKSPACE;
     if (!d_network || !d_out || (mode == 0 && !d_W) || (mode != 0 && !d_B)) return LYEM_ERR_INVALID;
-    if (n_src > 0x7fffffffLL / 2 || 2 * ld > 0x7fffffffLL || n_beams > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
+    if (n_src > 0x7fffffffLL || ld > 0x7fffffffLL || n_beams > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (split_mode(mode)) {
+        if ((reinterpret_cast<uintptr_t>(d_network) & 255) || (reinterpret_cast<uintptr_t>(d_B) & 255) ||
+            (reinterpret_cast<uintptr_t>(d_out) & 7))
+            return LYEM_ERR_INVALID;
+        return launch_sweep_tc(d_network, d_B, n_src, n_snk, ld, n_beams, mode == 3, d_out, ldc, s);
+    }
     std::lock_guard<std::mutex> lock(g_cublas_mutex);
     int err = 0;
     cublasHandle_t h = cublas_for_current_device(s, &err);
     if (err) return LYEM_ERR_CUDA;
+    const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
     for (int c = 0; c < 3; ++c) {
-        cublasStatus_t st = CUBLAS_STATUS_SUCCESS;
-        if (mode >= 3) {
-            const cudaDataType_t dt = mode == 3 ? CUDA_R_16BF : CUDA_R_16F;
-            const size_t plane = (size_t)ld * n_src;
-            const size_t part_b = (size_t)3 * n_src * n_beams;
-            float* T = static_cast<float*>(d_ws);
-            const float one = 1.f, zero = 0.f;
-            const int m = (int)ld, n = (int)n_beams, k = (int)n_src;
-            for (int q = 0; q < 3 && st == CUBLAS_STATUS_SUCCESS; ++q) {
-                const unsigned short* Ahi = reinterpret_cast<const unsigned short*>(d_network) + (6 * c + 2 * q) * plane;
-                const unsigned short* Bdup = reinterpret_cast<const unsigned short*>(d_B) + q * part_b;
-                const unsigned short* Blo = Bdup + (size_t)2 * n_src * n_beams;
-                float* C = T + (size_t)q * ld * n_beams;
-                // [hi | lo] x [hi ; hi] = hi*hi + lo*hi, then += hi*lo
-                st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, 2 * k, &one, Ahi, dt, m, Bdup, dt, 2 * k, &zero,
-                                  C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-                if (st == CUBLAS_STATUS_SUCCESS)
-                    st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, Ahi, dt, m, Blo, dt, k, &one, C,
-                                      CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-                note_launches(2);
-            }
-            if (st == CUBLAS_STATUS_SUCCESS) {
-                gauss_combine_kernel<<<sweep_blocks(ld * n_beams), 256, 0, s>>>(
-                    T, ld, n_beams, ldc, reinterpret_cast<float2*>(d_out) + (size_t)c * n_beams * ldc);
-                note_launches(1);
-                if (cudaGetLastError() != cudaSuccess) return LYEM_ERR_CUDA;
-            }
-        } else if (mode == 0) {
-            const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
-            const cuComplex* A = reinterpret_cast<const cuComplex*>(d_network) + (size_t)c * n_src * ld;
-            // the operand rows past n_snk are zero padding: run the aligned row count
-            st = cublasCgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)ld, (int)n_beams, (int)n_src, &one, A, (int)ld,
-                             reinterpret_cast<const cuComplex*>(d_W), (int)n_src, &zero,
-                             reinterpret_cast<cuComplex*>(d_out) + (size_t)c * n_beams * ldc, (int)ldc);
-            note_launches(1);
-        } else {
-            const cudaDataType_t dt = mode == 1 ? CUDA_R_16BF : CUDA_R_16F;
-            const size_t plane = (size_t)(2 * ld) * (2 * n_src);
-            const unsigned short* A = reinterpret_cast<const unsigned short*>(d_network) + (size_t)(2 * c) * plane;
-            const unsigned short* Alo = A + plane;
-            const unsigned short* B = reinterpret_cast<const unsigned short*>(d_B);
-            const unsigned short* Blo = B + (size_t)(2 * n_src) * n_beams;
-            float* C = d_out + (size_t)c * n_beams * 2 * ldc;
-            const float one = 1.f, zero = 0.f;
-            const int m = (int)(2 * ld), n = (int)n_beams, k = (int)(2 * n_src);  // padded rows are zero
-            const int lda = (int)(2 * ld), ldb = (int)(2 * n_src), ldo = (int)(2 * ldc);
-            st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, dt, lda, B, dt, ldb, &zero, C,
-                              CUDA_R_32F, ldo, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-            if (st == CUBLAS_STATUS_SUCCESS)
-                st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, dt, lda, Blo, dt, ldb, &one, C,
-                                  CUDA_R_32F, ldo, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-            if (st == CUBLAS_STATUS_SUCCESS)
-                st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, Alo, dt, lda, B, dt, ldb, &one, C,
-                                  CUDA_R_32F, ldo, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-            note_launches(3);
-        }
+        const cuComplex* A = reinterpret_cast<const cuComplex*>(d_network) + (size_t)c * n_src * ld;
+        // the operand rows past n_snk are zero padding: run the aligned row count
+        const cublasStatus_t st =
+            cublasCgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)ld, (int)n_beams, (int)n_src, &one, A, (int)ld,
+                        reinterpret_cast<const cuComplex*>(d_W), (int)n_src, &zero,
+                        reinterpret_cast<cuComplex*>(d_out) + (size_t)c * n_beams * ldc, (int)ldc);
+        note_launches(1);
         if (st != CUBLAS_STATUS_SUCCESS) return LYEM_ERR_CUDA;
     }
     return LYEM_OK;

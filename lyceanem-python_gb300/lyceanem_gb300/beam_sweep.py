@@ -5,10 +5,12 @@ The reference evaluates each excitation by re-running the whole model
 scene is formed once on the device (pair stage with unit excitations) and the
 sink fields of K excitation vectors are three complex GEMMs:
     E[m, k, c] = sum_n G[n, m, c] W[k, n].
-Modes: "fp32" (cublasCgemm), "bf16x3" and "fp16x3" (hi/lo split, three products
-on the tensor cores with FP32 accumulation), "bf16x3g" and "fp16x3g" (the same
-split with each complex product formed from three real products, Gauss's
-Gr Wr, Gi Wi, (Gr + Gi)(Wr + Wi): 6 instead of 8 M N K flops per component).
+Modes: "fp32" (cublasCgemm, the comparison path), "bf16x3g" and "fp16x3g"
+(this package's tcgen05 kernel: every real operand split into hi + lo halves,
+each complex product formed from three real products, Gauss's Gr Wr, Gi Wi,
+(Gr + Gi)(Wr + Wi), 6 instead of 8 M N K flops per component, each real product
+accumulated in FP32 as hi*hi + lo*hi + hi*lo; FP16 operands are scaled by powers
+of two so that no half overflows).
 """
 import ctypes
 
@@ -17,7 +19,12 @@ import torch
 from . import propagation as P
 from ._native import check, lib
 
-MODES = {"fp32": 0, "bf16x3": 1, "fp16x3": 2, "bf16x3g": 3, "fp16x3g": 4}
+MODES = {"fp32": 0, "bf16x3g": 3, "fp16x3g": 4}
+
+
+def set_k_tile(k_tile):
+    """Sources per pipeline stage of the tensor-core kernel: 64 (default) or 32."""
+    check(lib.lyem_sweep_set_k_tile(int(k_tile)), "sweep_set_k_tile")
 
 
 def _p(t):
@@ -39,7 +46,7 @@ def form_network(src, pol, snk, snk_n, *, beta, alpha=0.0, grid=None, tris=None,
 class BeamSweep:
     """A network prepared as the GEMM operand of one mode; run(W) evaluates K excitations at once."""
 
-    def __init__(self, network, mode="bf16x3"):
+    def __init__(self, network, mode="bf16x3g"):
         net = network.contiguous()
         assert net.dtype == torch.complex64 and net.dim() == 3 and net.shape[2] == 3
         self.mode = MODES[mode]

@@ -108,15 +108,25 @@ def test_header_compiles_as_c_and_links(tmp_path):
     assert int(out[0]) >= 100 and out[-3:] == ["41", "41", "13"]
 
 
-def test_sweep_three_product_modes_host_checks():
-    """The Gauss sweep modes (3, 4) need a workspace: sized by lyem_sweep_workspace_bytes, refused by the
-    entry point without one, and refused by the workspace-less lyem_sweep_run (host checks, no device call)."""
+def test_sweep_modes_host_checks():
+    """Beam-sweep sizes and argument checks (host only, no device call): operand sizes of the tensor-core
+    modes (3, 4: a 256-byte header and K-major planes with the source count rounded up to 8), no
+    workspace for any mode, the removed four-product modes (1, 2) and unknown modes refused, operands
+    that are not 256-byte aligned refused."""
     from lyceanem_gb300._native import lib
-    assert lib.lyem_sweep_workspace_bytes(1024, 16, 3) == 3 * 1024 * 16 * 4
-    assert lib.lyem_sweep_workspace_bytes(1024, 16, 1) == 0
-    assert lib.lyem_sweep_network_bytes(10, 16, 3) == 3 * 6 * 16 * 10 * 2
-    assert lib.lyem_sweep_weights_bytes(10, 4, 4) == 9 * 10 * 4 * 2
+    assert lib.lyem_sweep_workspace_bytes(1024, 16, 3) == 0
+    assert lib.lyem_sweep_network_bytes(10, 16, 3) == 256 + 18 * 16 * 16 * 2
+    assert lib.lyem_sweep_network_bytes(16, 16, 4) == 256 + 18 * 16 * 16 * 2
+    assert lib.lyem_sweep_network_bytes(10, 16, 0) == 3 * 10 * 16 * 8
+    assert lib.lyem_sweep_weights_bytes(10, 4, 4) == 256 + 6 * 4 * 16 * 2
+    assert lib.lyem_sweep_weights_bytes(10, 4, 0) == 0
+    for mode in (1, 2, 5):
+        assert lib.lyem_sweep_network_bytes(10, 16, mode) == 0
     fake = ctypes.c_void_p(256)
-    assert lib.lyem_sweep_run_ws(fake, 10, 16, 16, None, fake, 4, 3, fake, 16, None, 0, None) == 6  # workspace
-    assert lib.lyem_sweep_run(fake, 10, 16, 16, None, fake, 4, 3, fake, 16, None) == 1  # invalid: needs _ws
-    assert lib.lyem_sweep_run_ws(fake, 10, 16, 16, None, fake, 4, 5, fake, 16, None, 0, None) == 1  # no mode 5
+    odd = ctypes.c_void_p(256 + 64)
+    assert lib.lyem_sweep_run_ws(fake, 10, 16, 16, None, fake, 4, 1, fake, 16, None, 0, None) == 1  # mode 1 gone
+    assert lib.lyem_sweep_run(fake, 10, 16, 16, None, fake, 4, 5, fake, 16, None) == 1  # no mode 5
+    assert lib.lyem_sweep_run(odd, 10, 16, 16, None, fake, 4, 3, fake, 16, None) == 1  # unaligned network
+    assert lib.lyem_sweep_prepare_weights(fake, 10, 4, 3, odd, None) == 1  # unaligned weight operand
+    assert lib.lyem_sweep_set_k_tile(48) == 1
+    assert lib.lyem_sweep_set_k_tile(64) == 0

@@ -483,8 +483,10 @@ def test_direction_order():
     _no_device_errors()
 
 
-@pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3", 1e-4), ("fp16x3", 1e-5), ("bf16x3g", 1e-4),
-                                      ("fp16x3g", 2e-5)])
+SWEEP_TOL = 1e-4  # relative Frobenius error of a mixed-precision sweep against FP64 (the stated bar)
+
+
+@pytest.mark.parametrize("mode,tol", [("fp32", 2e-6), ("bf16x3g", SWEEP_TOL), ("fp16x3g", SWEEP_TOL)])
 def test_beam_sweep_modes_against_fp64(mode, tol):
     """Beam sweep of a formed network against a complex128 product of the same network."""
     from lyceanem_gb300 import beam_sweep as BS
@@ -505,6 +507,66 @@ def test_beam_sweep_modes_against_fp64(mode, tol):
     om = O.Grid(O.pack_triangles(s.verts, s.faces), 0.5).mask(s.src, s.snk, self_to_self=True)
     Go = O.pair_field(s.src, np.tile(s.pol, (s.src.shape[0], 1)), s.snk, s.snk_n, om, 0.0, beta)
     assert _pair_rel(G.cpu().numpy(), Go, s.src, s.snk, np.tile(s.pol, (s.src.shape[0], 1)), beta) < FIELD_TOL
+
+
+def _sweep_vs_fp64(G, W, mode):
+    from lyceanem_gb300 import beam_sweep as BS
+    sw = BS.BeamSweep(G, mode)
+    E = sw.fields(sw.run(W)).cpu().numpy()
+    ref = torch.einsum("nmc,kn->mkc", G.cpu().to(torch.complex128), W.cpu().to(torch.complex128)).numpy()
+    _no_device_errors()
+    return float(np.linalg.norm(E - ref) / np.linalg.norm(ref)), E, ref
+
+
+@pytest.mark.parametrize("k_tile", [64, 32])
+@pytest.mark.parametrize("n_src,n_snk,n_beams", [(13, 300, 5), (200, 129, 257), (64, 128, 256)])
+def test_beam_sweep_tensor_core_shapes(k_tile, n_src, n_snk, n_beams):
+    """The tensor-core kernel on ragged sizes (sources not a multiple of 8 or of the k-tile, sinks and
+    beams across tile edges) and on exact tile multiples, both k-tiles, against a complex128 product;
+    every output column and row inside the sizes is written."""
+    from lyceanem_gb300 import beam_sweep as BS
+    g = torch.Generator().manual_seed(n_src * 7 + n_beams)
+    G = torch.randn((n_src, n_snk, 3), dtype=torch.complex64, generator=g).cuda()
+    W = torch.exp(2j * np.pi * torch.rand((n_beams, n_src), generator=g)).to(torch.complex64).cuda()
+    BS.set_k_tile(k_tile)
+    try:
+        for mode in ("bf16x3g", "fp16x3g"):
+            err, E, ref = _sweep_vs_fp64(G, W, mode)
+            assert err < SWEEP_TOL, (mode, err)
+            # no entry is left unwritten (a stale tile would show as a large per-entry error)
+            assert np.abs(E - ref).max() < 1e-3 * np.abs(ref).max(), mode
+    finally:
+        BS.set_k_tile(64)
+
+
+@pytest.mark.parametrize("scale", [1e-8, 1e-4, 1e4])
+def test_beam_sweep_fp16_scaling(scale):
+    """FP16 halves of a network of very small or very large entries: the power-of-two scaling keeps the
+    halves out of FP16's subnormal and overflow ranges, so the error stays at the O(1) network's."""
+    g = torch.Generator().manual_seed(5)
+    G = (torch.randn((96, 700, 3), dtype=torch.complex64, generator=g) * scale).cuda()
+    W = (torch.exp(2j * np.pi * torch.rand((40, 96), generator=g)) * 0.01).to(torch.complex64).cuda()
+    for mode in ("fp16x3g", "bf16x3g"):
+        err, _, _ = _sweep_vs_fp64(G, W, mode)
+        assert err < SWEEP_TOL, (mode, scale, err)
+
+
+def test_beam_sweep_repeat_and_reuse():
+    """Two runs of one prepared sweep give identical results (the kernel writes every output once, from
+    a fixed accumulation order), and a second weight set reuses the operand."""
+    from lyceanem_gb300 import beam_sweep as BS
+    g = torch.Generator().manual_seed(9)
+    G = torch.randn((40, 333, 3), dtype=torch.complex64, generator=g).cuda()
+    W1 = torch.randn((70, 40), dtype=torch.complex64, generator=g).cuda()
+    W2 = torch.randn((70, 40), dtype=torch.complex64, generator=g).cuda()
+    sw = BS.BeamSweep(G, "bf16x3g")
+    a = sw.run(W1).clone()
+    b = sw.run(W1).clone()
+    assert torch.equal(sw.fields(a), sw.fields(b))
+    c = sw.fields(sw.run(W2)).cpu().numpy()
+    ref = torch.einsum("nmc,kn->mkc", G.cpu().to(torch.complex128), W2.cpu().to(torch.complex128)).numpy()
+    assert np.linalg.norm(c - ref) / np.linalg.norm(ref) < SWEEP_TOL
+    _no_device_errors()
 
 
 @pytest.mark.parametrize("case", ["direct", "random"])
