@@ -229,7 +229,7 @@ __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView
             continue;
         }
         const float* so = spos + 3 * n;
-        if (!walk_begin(G, w, __ldg(so), __ldg(so + 1), __ldg(so + 2), ex, ey, ez)) {
+        if (!walk_begin<CULL>(G, w, __ldg(so), __ldg(so + 1), __ldg(so + 2), ex, ey, ez)) {
             vis |= 1ull << s;
             continue;
         }

@@ -40,6 +40,30 @@ __device__ __forceinline__ Ray make_ray(float ox, float oy, float oz, float ex, 
     return r;
 }
 
+// The numba engine's ray set-up (charge_rays_environment1Dv2 -> calc_dv_norm,
+// lyceanem/raycasting/rayfunctions.py:1790-1842, lyceanem/utility/math_functions.py:149-156):
+// numpy float32 arithmetic on the host, nothing fused: the squared length is
+// ((rx*rx + ry*ry) + rz*rz) with every step rounded, then sqrt and one division
+// per component.
+__device__ __forceinline__ Ray make_ray_numba(float ox, float oy, float oz, float ex, float ey, float ez) {
+    float rx = __fsub_rn(ex, ox), ry = __fsub_rn(ey, oy), rz = __fsub_rn(ez, oz);
+    float w2 = __fadd_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)), __fmul_rn(rz, rz));
+    float w = __fsqrt_rn(w2);
+    Ray r;
+    r.dx = __fdiv_rn(rx, w);
+    r.dy = __fdiv_rn(ry, w);
+    r.dz = __fdiv_rn(rz, w);
+    r.len = w;
+    return r;
+}
+
+// Ray of a visibility test: the CUDA engine's set-up in the culling mode, the
+// numba engine's in the non-culling mode (the mode that reproduces that engine).
+template <bool CULL>
+__device__ __forceinline__ Ray vis_ray(float ox, float oy, float oz, float ex, float ey, float ez) {
+    return CULL ? make_ray(ox, oy, oz, ex, ey, ez) : make_ray_numba(ox, oy, oz, ex, ey, ez);
+}
+
 // Per (source, triangle) quantities of the Moller-Trumbore test that do not
 // depend on the ray direction: tvec = o - v0, qvec = tvec x e1, tq = e2 . qvec.
 // Computing them once per source and reusing them gives the same bits as
@@ -87,6 +111,30 @@ __device__ __forceinline__ bool outside_unit(float x, float A) {
     return sx < __fmul_rn(sa, -0x1p-20f) || sx > __fmaf_rn(sa, 0x1p-19f, sa);
 }
 
+// The numba engine's decisions after the determinant (rayfunctions.py:55-100):
+// there F = 1.0 / A, U = F u, V = F v and t = F w are FP64 (the float64 literal
+// promotes the float32 determinant) and are compared in FP64.  With u, v and A
+// float32 (A != 0), the U and V sign tests and U > 1 are exact FP32 comparisons:
+//   F u < 0  <=>  u / A < 0: no FP64 product of float32-derived values
+//             underflows, so the sign survives rounding (u = +-0 gives +-0);
+//   F u > 1  <=>  s u > |A| (s = sign A): for float32 u != A of one sign,
+//             |u / A - 1| >= 2^-25, far beyond the 2^-52 relative error of F u,
+//             and u == A gives F u in {1, 1 - 2^-53}.
+// U + V > 1 and the t range are evaluated in FP64 as there.  A NaN numerator
+// fails every comparison, as in FP64; with a NaN determinant numba's t is NaN
+// and the test is a miss, which an early miss here matches.
+__device__ __forceinline__ bool ratio_negative(float x, float A) { return A < 0.f ? x > 0.f : x < 0.f; }
+__device__ __forceinline__ bool ratio_above_one(float x, float A) { return (A < 0.f ? -x : x) > fabsf(A); }
+
+__device__ __forceinline__ bool numba_tail(float A, float u, float v, float w, float len, float eps) {
+    const double F = 1.0 / (double)A;
+    const double U = F * (double)u, V = F * (double)v;
+    if (U + V > 1.0) return false;
+    const double t = F * (double)w;
+    const double two_eps = 2.0 * (double)eps;
+    return (t > two_eps) && (t < (double)len - two_eps);
+}
+
 // hit() with the per-source quantities precomputed.
 template <bool CULL>
 __device__ __forceinline__ bool hit_pre(const Ray& r, const TriPre& p, float eps) {
@@ -97,6 +145,13 @@ __device__ __forceinline__ bool hit_pre(const Ray& r, const TriPre& p, float eps
     float pz = __fmaf_rn(r.dx, e2y, -__fmul_rn(r.dy, e2x));
     float A = __fmaf_rn(e1z, pz, __fmaf_rn(e1y, py, __fmul_rn(e1x, px)));
     if (det_rejects<CULL>(A, eps)) return false;
+    if (!CULL) {
+        const float u = __fmaf_rn(p.c.x, pz, __fmaf_rn(p.b.w, py, __fmul_rn(p.b.z, px)));
+        if (ratio_negative(u, A) || ratio_above_one(u, A)) return false;
+        const float v = __fmaf_rn(r.dz, p.c.w, __fmaf_rn(r.dy, p.c.z, __fmul_rn(r.dx, p.c.y)));
+        if (ratio_negative(v, A)) return false;
+        return numba_tail(A, u, v, p.d.x, r.len, eps);
+    }
     float F = __frcp_rn(A);
     float U = __fmul_rn(F, __fmaf_rn(p.c.x, pz, __fmaf_rn(p.b.w, py, __fmul_rn(p.b.z, px))));
     if (U < 0.f || U > 1.f) return false;
@@ -118,6 +173,15 @@ __device__ __forceinline__ bool hit_full(const Ray& r, float ox, float oy, float
     if (det_rejects<CULL>(A, eps)) return false;
     float tx = __fsub_rn(ox, v0.x), ty = __fsub_rn(oy, v0.y), tz = __fsub_rn(oz, v0.z);
     const float u = __fmaf_rn(tz, pz, __fmaf_rn(ty, py, __fmul_rn(tx, px)));
+    if (!CULL) {
+        if (ratio_negative(u, A) || ratio_above_one(u, A)) return false;
+        const float qx = __fmaf_rn(ty, e1.z, -__fmul_rn(tz, e1.y));
+        const float qy = __fmaf_rn(tz, e1.x, -__fmul_rn(tx, e1.z));
+        const float qz = __fmaf_rn(tx, e1.y, -__fmul_rn(ty, e1.x));
+        const float v = __fmaf_rn(r.dz, qz, __fmaf_rn(r.dy, qy, __fmul_rn(r.dx, qx)));
+        if (ratio_negative(v, A)) return false;
+        return numba_tail(A, u, v, __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx))), r.len, eps);
+    }
     if (outside_unit(u, A)) return false;
     float F = __frcp_rn(A);
     float U = __fmul_rn(F, u);

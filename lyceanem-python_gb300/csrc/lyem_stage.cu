@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
             const bool mine = (pending >> s) & 1u;
             if (!__syncthreads_or(mine)) continue;
             if (mine) {
-                const Ray r = make_ray(ox, oy, oz, ex, ey, ez);
+                const Ray r = vis_ray<CULL>(ox, oy, oz, ex, ey, ez);
                 int j = 0;
                 bool hitany = false;
                 for (; j < cnt; ++j) {
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == k
             const long long n = src_index(s);
             if (!m_ok || (p.skip_diag && n == m)) continue;
             const float* so = p.src_pos + 3 * n;
-            walk_ray(w, so[0], so[1], so[2], ex, ey, ez);
+            walk_ray<CULL>(w, so[0], so[1], so[2], ex, ey, ez);
             const int hint = s_hint[s];
             bool hit = false;
             if (hint >= 0) {  // a hit on any triangle blocks the segment, walked or not
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == k
                 const long long n = src_index(s);
                 if (p.skip_diag && n == m) continue;
                 const float* so = p.src_pos + 3 * n;
-                if (walk_begin(p, w, so[0], so[1], so[2], ex, ey, ez)) { has = true; return; }
+                if (walk_begin<CULL>(p, w, so[0], so[1], so[2], ex, ey, ez)) { has = true; return; }
             }
         };
         const unsigned full = 0xffffffffu;

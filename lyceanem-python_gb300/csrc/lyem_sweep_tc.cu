@@ -244,6 +244,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll 1
                 for (int j = 0; j < kBN / 32; ++j) {
                     float v[32];
+                    __syncwarp();  // tcgen05.ld is a .sync.aligned warp instruction
                     tc::tmem_ld32(tmem + lane_off + col0 + (uint32_t)j * 32u, v);
                     if (m < p.n_snk) {
 #pragma unroll
@@ -261,6 +262,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int j = 0; j < kBN / 32; ++j) {
                 float a[32], b[32];
                 const uint32_t ta = tmem + lane_off + (uint32_t)j * 32u, tb = ta + (uint32_t)kBN;
+                __syncwarp();
                 tc::tmem_ld32x2(ta, tb, a, b);
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
@@ -271,6 +273,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 tc::tmem_st32(ta, a);
                 tc::tmem_st32(tb, b);
             }
+            __syncwarp();
             tc::tmem_wait_st();
             signal(bar(MID_DONE));  // pass s may now accumulate T3 onto -(T1 + T2)
             write_part(0u, 0);

@@ -65,10 +65,11 @@ __device__ __forceinline__ void walk_enter(const GP& p, Walk& w, int c) {
     w.q1 = q < q1 ? q1 : q;
 }
 
-// The segment o -> e of a walk (origin and ray); enough for walk_test_ref.
+// The segment o -> e of a walk (origin and visibility ray of the mode); enough for walk_test_ref.
+template <bool CULL>
 __device__ __forceinline__ void walk_ray(Walk& w, float ox, float oy, float oz, float ex, float ey, float ez) {
     w.ox = ox; w.oy = oy; w.oz = oz;
-    w.r = make_ray(ox, oy, oz, ex, ey, ez);
+    w.r = vis_ray<CULL>(ox, oy, oz, ex, ey, ez);
 }
 
 // Enters the grid along the segment set by walk_ray; false if it misses the grid box.
@@ -102,10 +103,10 @@ __device__ __forceinline__ bool walk_setup(const GP& p, Walk& w) {
 }
 
 // Starts the walk of segment o -> e; false if the segment misses the grid box.
-template <class GP>
+template <bool CULL, class GP>
 __device__ __forceinline__ bool walk_begin(const GP& p, Walk& w, float ox, float oy, float oz, float ex,
                                            float ey, float ez) {
-    walk_ray(w, ox, oy, oz, ex, ey, ez);
+    walk_ray<CULL>(w, ox, oy, oz, ex, ey, ez);
     return walk_setup(p, w);
 }
 

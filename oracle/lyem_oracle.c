@@ -86,10 +86,34 @@ static inline void orc_ray(const float *o, const float *e, f3 *d, float *len) {
     *len = w;
 }
 
+/* The numba engine's ray set-up: numpy float32 on the host with nothing fused
+ * (calc_dv_norm, lyceanem/utility/math_functions.py:149-156, called by
+ * charge_rays_environment1Dv2, lyceanem/raycasting/rayfunctions.py:1790-1842):
+ * ((rx*rx + ry*ry) + rz*rz), sqrt, one division per component. */
+static inline void orc_ray_numba(const float *o, const float *e, f3 *d, float *len) {
+    float rx = e[0] - o[0], ry = e[1] - o[1], rz = e[2] - o[2];
+    float w2 = (rx * rx + ry * ry) + rz * rz;
+    float w = sqrtf(w2);
+    d->x = rx / w;
+    d->y = ry / w;
+    d->z = rz / w;
+    *len = w;
+}
+
+/* Visibility ray of a mode: the CUDA engine's with culling, the numba engine's without. */
+static inline void orc_vis_ray(const float *o, const float *e, int cull, f3 *d, float *len) {
+    if (cull)
+        orc_ray(o, e, d, len);
+    else
+        orc_ray_numba(o, e, d, len);
+}
+
 /* Moller-Trumbore test (raycasting.cuh:19-68).  cull != 0 is the CUDA engine
- * (|A| < eps or A < 0 is a miss); cull == 0 is the numba engine
- * (rayfunctions.py:55-60, only |A| < eps is a miss).  F = 1/A is the correctly
- * rounded FP32 reciprocal, which equals the reference's (float)(1.0/(double)A). */
+ * (|A| < eps or A < 0 is a miss; F = 1/A is the correctly rounded FP32
+ * reciprocal, which equals the reference's (float)(1.0/(double)A)).  cull == 0
+ * is the numba engine (rayfunctions.py:37-104): only |A| < eps is a miss, and
+ * F = 1.0 / A, U, V and t are FP64 there (the float64 literal promotes the
+ * float32 determinant) and compared in FP64; the numerators stay FP32. */
 int orc_hit(f3 d, float len, f3 o, f3 e1, f3 e2, f3 v0, int cull, float eps) {
     f3 p = cross3(d, e2);
     float A = dot3(e1, p);
@@ -97,6 +121,16 @@ int orc_hit(f3 d, float len, f3 o, f3 e1, f3 e2, f3 v0, int cull, float eps) {
         if (!(A >= eps)) return 0;
     } else {
         if (fabsf(A) < eps) return 0;
+        f3 t = sub3(o, v0);
+        double F = 1.0 / (double)A;
+        double U = F * (double)dot3(t, p);
+        if (U < 0.0 || U > 1.0) return 0;
+        f3 q = cross3(t, e1);
+        double V = F * (double)dot3(d, q);
+        if (V < 0.0 || (U + V) > 1.0) return 0;
+        double tt = F * (double)dot3(e2, q);
+        double two_eps = 2.0 * (double)eps;
+        return (tt > two_eps) && (tt < ((double)len - two_eps));
     }
     f3 t = sub3(o, v0);
     float F = 1.0f / A;
@@ -138,7 +172,7 @@ void orc_mask_brute(const float *src, int64_t N, const float *snk, int64_t M, co
         if (!(skip_diag && n == m)) {
             f3 d;
             float len;
-            orc_ray(src + 3 * n, snk + 3 * m, &d, &len);
+            orc_vis_ray(src + 3 * n, snk + 3 * m, cull, &d, &len);
             f3 o = mk3(src[3 * n], src[3 * n + 1], src[3 * n + 2]);
             for (int64_t t = 0; t < T; ++t) {
                 if (orc_hit_packed(d, len, o, tris + 12 * t, cull, eps)) { vis = 0; break; }
@@ -307,7 +341,7 @@ void orc_mask_grid(void *h, const float *src, int64_t N, const float *snk, int64
         if (!(skip_diag && n == m)) {
             f3 d;
             float len;
-            orc_ray(src + 3 * n, snk + 3 * m, &d, &len);
+            orc_vis_ray(src + 3 * n, snk + 3 * m, cull, &d, &len);
             vis = !orc_grid_blocked(g, src + 3 * n, snk + 3 * m, d, len, cull, eps, NULL);
         }
         mask[i] = vis;
@@ -404,7 +438,7 @@ void orc_sink_field(const float *src, const double *srcE, const double *srcW, in
             } else if (!(skip_diag && n == m)) {
                 f3 d;
                 float len;
-                orc_ray(src + 3 * n, snk + 3 * m, &d, &len);
+                orc_vis_ray(src + 3 * n, snk + 3 * m, cull, &d, &len);
                 if (grid) {
                     vis = !orc_grid_blocked((const orc_grid *)grid, src + 3 * n, snk + 3 * m, d, len,
                                             cull, eps, &tests_total);

@@ -11,6 +11,13 @@ Fixtures:
                           reference's Tile_acceleration_structure.__init__
                           (lyceanem/models/acceleration_structures.py:55-71), imported
                           with a recording stand-in for its compiled `em` module
+  excitation.npz          the seven excitation_function known-answer cases of
+                          lyceanem/tests/test_base_classes.py:70-152 (desired vector, pose
+                          rotation, stated answer) and, for them and for steered and
+                          area-weighted apertures, the outputs of the reference's own
+                          excitation_function (lyceanem/electromagnetics/emfunctions.py:9-82)
+                          and helpers, executed from their source text (the modules
+                          themselves import numba and pyvista, absent here)
 Usage: python tests/golden/make_golden.py [reference_root]
 """
 import ast
@@ -108,8 +115,99 @@ def tile_structure():
              n_cells=np.array(out_n), values=np.array(out_vals, np.float64))
 
 
+def _functions(path, names, strip_decorators=True):
+    """Source of the named top-level functions of a reference file, decorators (numba's njit) and
+    function-local imports removed, as one module to exec."""
+    class _NoImports(ast.NodeTransformer):
+        def visit_Import(self, node):
+            return ast.Pass()
+
+        visit_ImportFrom = visit_Import
+
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", SyntaxWarning)  # escape sequences in the reference's docstrings
+        tree = ast.parse(open(path).read())
+    out = []
+    for node in tree.body:
+        if isinstance(node, ast.FunctionDef) and node.name in names:
+            if strip_decorators:
+                node.decorator_list = []
+            out.append(_NoImports().visit(node))
+    return ast.fix_missing_locations(ast.Module(body=out, type_ignores=[]))
+
+
+class _PointCloud:
+    def __init__(self, points, normals, area=None):
+        self.points = points
+        self.point_data = {"Normals": normals}
+        if area is not None:
+            self.point_data["Area"] = area
+
+
+def excitation_cases():
+    import scipy.constants
+    from scipy.spatial import distance
+    from scipy.spatial.transform import Rotation as R
+    ns = {"np": np, "scipy": scipy, "distance": distance, "__name__": "reference_functions"}
+    for rel, names in ((("electromagnetics", "empropagation.py"), {"vector_mapping", "calculate_conformalVectors"}),
+                       (("electromagnetics", "beamforming.py"), {"WavefrontWeights", "ArbitaryCoherenceWeights"}),
+                       (("utility", "math_functions.py"), {"discrete_transmit_power"}),
+                       (("electromagnetics", "emfunctions.py"), {"excitation_function"})):
+        exec(compile(_functions(os.path.join(PKG, *rel), names), rel[-1], "exec"), ns)
+    ref_excitation = ns["excitation_function"]
+    # the known-answer cases: one point at +x of a unit cube with normal +x, antenna pose rotated
+    src = open(os.path.join(PKG, "tests", "test_base_classes.py")).read()
+    tree = ast.parse(src)
+    names, desired, rot, stated, outputs = [], [], [], [], []
+
+    class _Antenna:
+        def __init__(self):
+            self.pose = np.eye(4)
+
+    for fn in tree.body:
+        if not (isinstance(fn, ast.FunctionDef) and fn.name.startswith("test_excitation_function")):
+            continue
+        case = {"np": np, "R": R, "standard_antenna": _Antenna()}
+        for st in fn.body:
+            if isinstance(st, ast.Assign):
+                exec(compile(ast.Module(body=[st], type_ignores=[]), "<case>", "exec"), case)
+        pose = case["standard_antenna"].pose
+        pt = (pose @ np.array([0.5, 0.0, 0.0, 1.0]))[:3].reshape(1, 3)
+        nrm = (pose @ np.array([1.0, 0.0, 0.0, 0.0]))[:3].reshape(1, 3)
+        names.append(fn.name)
+        desired.append(case["desired_E_vector"])
+        rot.append(pose[:3, :3])
+        stated.append(case["final_vector"].reshape(3))
+        outputs.append(np.asarray(ref_excitation(_PointCloud(pt, nrm), case["desired_E_vector"])).reshape(3))
+    # steered and area-weighted apertures through the same function
+    rng = np.random.default_rng(31)
+    ap_pts = np.stack(np.meshgrid(np.arange(4) * 0.015, np.arange(4) * 0.015, [0.0]), -1).reshape(-1, 3)
+    ap_n = np.tile(np.array([[0.0, 0.0, 1.0]]), (16, 1))
+    area = rng.uniform(0.5, 2.0, 16) * 1e-4
+    steer = np.array([[0.3, -0.2, 0.93]])
+    target = np.array([[0.4, 0.1, 2.0]])
+    extra = []
+    for label, kw, cloud in (
+            ("wavefront_area", dict(phase_shift="wavefront", wavelength=0.03, steering_vector=steer,
+                                    transmit_power=2.5), _PointCloud(ap_pts, ap_n, area)),
+            ("coherence", dict(phase_shift="coherence", wavelength=0.03, steering_vector=target),
+             _PointCloud(ap_pts, ap_n)),
+            ("no_projection", dict(local_projection=False, wavelength=0.05, transmit_power=10.0),
+             _PointCloud(ap_pts, ap_n, area))):
+        d = np.array([[1.0, 0.5j, 0.0]], dtype=np.complex64) if label == "no_projection" else \
+            np.array([0.0, 1.0, 0.0], dtype=np.complex64)
+        extra.append((label, d.reshape(-1)[:3], kw, np.asarray(ref_excitation(cloud, d, **kw))))
+    np.savez(os.path.join(HERE, "excitation.npz"), names=np.array(names), desired=np.stack(desired),
+             rotation=np.stack(rot), stated=np.stack(stated), reference=np.stack(outputs),
+             ap_points=ap_pts, ap_normals=ap_n, ap_area=area, steer=steer, target=target,
+             extra_names=np.array([e[0] for e in extra]), extra_desired=np.stack([e[1] for e in extra]),
+             extra_reference=np.stack([e[3] for e in extra]))
+
+
 if __name__ == "__main__":
     convert_triangles()
     vector_mapping_cases()
     tile_structure()
+    excitation_cases()
     print("golden fixtures written to", HERE)

@@ -41,3 +41,38 @@ def test_tile_structure_geometry_golden():
         g = tile_geometry(pts, int(n_cells))
         got = np.array([g[k] for k in keys], np.float64)
         assert np.array_equal(got, vals), (got, vals)
+
+
+class _Cloud:
+    def __init__(self, points, normals, area=None):
+        self.points = points
+        self.point_data = {"Normals": normals}
+        if area is not None:
+            self.point_data["Area"] = area
+
+
+def test_excitation_function_golden():
+    """The seven known-answer cases of lyceanem/tests/test_base_classes.py:70-152 (one point at +x of a
+    unit cube, normal +x, antenna pose rotated) and steered / area-weighted apertures, against the outputs
+    of the reference's own excitation_function.  The stated answers are unit vectors; the reference
+    function scales them to 1 W over the default area (|E| = sqrt(4 * 120 pi)), so they pin the direction."""
+    from lyceanem_gb300.excitation import excitation_function
+    d = np.load(os.path.join(GOLD, "excitation.npz"))
+    for i in range(len(d["names"])):
+        Rm = d["rotation"][i]
+        pt = (Rm @ np.array([0.5, 0.0, 0.0])).reshape(1, 3)
+        nrm = (Rm @ np.array([1.0, 0.0, 0.0])).reshape(1, 3)
+        got = excitation_function(_Cloud(pt, nrm), d["desired"][i]).reshape(3)
+        np.testing.assert_allclose(got, d["reference"][i], rtol=1e-6, atol=1e-5, err_msg=str(d["names"][i]))
+        st = d["stated"][i]
+        np.testing.assert_allclose(got / np.linalg.norm(got), st / np.linalg.norm(st), atol=1e-6)
+        assert abs(np.linalg.norm(got) - np.sqrt(4 * 120 * np.pi)) < 1e-4
+    kws = {"wavefront_area": dict(phase_shift="wavefront", wavelength=0.03, steering_vector=d["steer"],
+                                  transmit_power=2.5),
+           "coherence": dict(phase_shift="coherence", wavelength=0.03, steering_vector=d["target"]),
+           "no_projection": dict(local_projection=False, wavelength=0.05, transmit_power=10.0)}
+    for i, name in enumerate(d["extra_names"]):
+        area = None if name == "coherence" else d["ap_area"]
+        desired = d["extra_desired"][i].reshape(1, 3) if name == "no_projection" else d["extra_desired"][i]
+        got = excitation_function(_Cloud(d["ap_points"], d["ap_normals"], area), desired, **kws[str(name)])
+        np.testing.assert_allclose(got, d["extra_reference"][i], rtol=2e-6, atol=1e-4, err_msg=str(name))

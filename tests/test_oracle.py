@@ -171,3 +171,25 @@ def test_numba_path_product_factorises():
     assert np.all(full[:, 1] != full[:, 2])
     net = O.path_field(idx, pos, nrm, w, N, M, 0.0, 60.0)
     assert np.all(np.isfinite(net))
+
+
+def test_numba_ratio_decisions_exact():
+    """The non-culling kernels decide the numba engine's U < 0, U > 1 and V < 0 (there F = 1.0 / A and
+    U = F * u in FP64, lyceanem/raycasting/rayfunctions.py:55-100) by comparing the float32 numerator with
+    the float32 determinant: u / A < 0 as a sign test, u / A > 1 as sign(A) * u > |A|.  Both agree with the
+    FP64 evaluation on random and adversarial float32 pairs: u == A and its neighbours, both signs, zeros,
+    tiny and huge magnitudes."""
+    rng = np.random.default_rng(0)
+    n = 200000
+    A = (rng.choice([-1.0, 1.0], n) * 2.0 ** rng.uniform(-60, 60, n)).astype(np.float32)
+    near = np.stack([A, np.nextafter(A, np.float32(np.inf)), np.nextafter(A, np.float32(-np.inf)), -A,
+                     np.zeros_like(A), -np.zeros_like(A),
+                     (A * rng.uniform(0.999999, 1.000001, n)).astype(np.float32),
+                     (rng.choice([-1.0, 1.0], n) * 2.0 ** rng.uniform(-149, 127, n)).astype(np.float32)])
+    for u in near:
+        F = 1.0 / A.astype(np.float64)
+        U = F * u.astype(np.float64)
+        neg = np.where(A < 0, u > 0, u < 0)
+        above = np.where(A < 0, -u, u) > np.abs(A)
+        assert np.array_equal(neg, U < 0)
+        assert np.array_equal(above, U > 1)
