@@ -99,19 +99,55 @@ def path_times(full_index, pos, nrm, weights, n_src, n_snk, alpha, beta, magneti
     return amp, arrival, pair
 
 
-def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples):
-    """float64 [n_src, n_snk, num_samples, 3] (CUDA): each row's excitation, scaled by its magnitudes,
-    starting at floor((arrival - wake) / (1 / sampling_freq)) samples and cut at num_samples, with
-    wake = the earliest arrival; returned with wake.  Built as an amplitude histogram of arrival
-    samples per (source, sink) convolved with the excitation (FFT)."""
+MAP_BYTES_LIMIT = 1e9  # TimeDomainv3 splits the sources into chunks when its float64 map exceeds this
+
+
+def start_samples(arrival, src_of_row, n_src, n_snk, num_samples, sampling_freq, map_bytes_limit=MAP_BYTES_LIMIT):
+    """(start sample of each row's excitation, int64 [R]; the reported wake time) as TimeDomainv3 sets them
+    (lyceanem/electromagnetics/empropagation.py:2955-3170), with the wake times taken before any row is
+    placed (there an atomic minimum synchronised only within a thread block):
+    - a map (n_src x n_snk x num_samples x 3 float64) of at most map_bytes_limit bytes has one wake time,
+      min(1 s, the arrivals); a row starts floor((arrival - wake) / step) samples in;
+    - a larger map splits the sources into ceil(bytes / limit) chunks (np.linspace bounds): chunk 0's wake
+      is min(1 s, its arrivals), chunk n's min(chunk 0's wake, its arrivals), and a row starts relative to
+      its chunk's wake.  When the chunk wakes differ by a sample or more the reference shifts each chunk by
+      round((wake_n - min wake) / step) samples to align them (its copy for the chunk at the minimum uses the
+      empty slice :-0, so there the reference raises); here that shift is applied.  The reported wake is
+      chunk 0's."""
+    dev = arrival.device
+    step = 1.0 / sampling_freq
+    nbytes = float(n_src) * n_snk * num_samples * 3 * 8
+    step_t = torch.tensor(step, dtype=torch.float64, device=dev)
+    if nbytes <= map_bytes_limit:
+        wake = min(1.0, float(arrival.min().item())) if arrival.numel() else 1.0
+        return torch.div(arrival - wake, step_t, rounding_mode="floor").to(torch.int64), wake
+    n_chunks = int(np.ceil(nbytes / map_bytes_limit))
+    bounds = np.linspace(0, n_src, n_chunks + 1).astype(np.int32)
+    chunk = torch.bucketize(src_of_row.to(torch.int64), torch.as_tensor(bounds[1:-1], dtype=torch.int64, device=dev),
+                            right=True)
+    first = torch.full((n_chunks,), float("inf"), dtype=torch.float64, device=dev)
+    first = first.scatter_reduce(0, chunk, arrival, reduce="amin").cpu().numpy()
+    wakes = np.empty(n_chunks)
+    wakes[0] = min(1.0, first[0])
+    wakes[1:] = np.minimum(wakes[0], first[1:])
+    shift = np.zeros(n_chunks, np.int64)
+    if np.max((wakes - np.min(wakes)) / step) >= 1.0:
+        shift = np.round((wakes - np.min(wakes)) / step).astype(np.int64)
+    w_row = torch.as_tensor(wakes, device=dev)[chunk]
+    s_row = torch.as_tensor(shift, device=dev)[chunk]
+    return torch.div(arrival - w_row, step_t, rounding_mode="floor").to(torch.int64) + s_row, float(wakes[0])
+
+
+def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples, map_bytes_limit=MAP_BYTES_LIMIT):
+    """float64 [n_src, n_snk, num_samples, 3]: each row's excitation, scaled by its magnitudes, starting at
+    the sample start_samples gives it and cut at num_samples; returned with the reported wake time.  Built
+    as an amplitude histogram of start samples per (source, sink) convolved with the excitation (FFT)."""
     dev = amp.device
     S = int(num_samples)
     exc = torch.as_tensor(np.asarray(excitation, np.float64), device=dev).reshape(-1)
     if arrival.numel() == 0:
         return torch.zeros((n_src, n_snk, S, 3), dtype=torch.float64, device=dev), 1.0
-    wake = float(arrival.min().item())
-    step = torch.tensor(1.0 / sampling_freq, dtype=torch.float64, device=dev)
-    t0 = torch.div(arrival - wake, step, rounding_mode="floor").to(torch.int64)
+    t0, wake = start_samples(arrival, pair[:, 0], n_src, n_snk, S, sampling_freq, map_bytes_limit)
     keep = t0 < S
     h = torch.zeros((n_src * n_snk * S, 3), dtype=torch.float64, device=dev)
     flat = (pair[:, 0].long() * n_snk + pair[:, 1].long()) * S + t0
@@ -127,9 +163,9 @@ def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_sa
 def TimeDomainv3(source_num, sink_num, point_informationv2, full_index, scattering_coefficient, wavelength,
                  excitation_signal, sampling_freq, num_samples, alpha, beta):
     """(time_map float64 [source_num, sink_num, num_samples, 3], wake_times [1]) of
-    lyceanem/electromagnetics/empropagation.py:2910-3170 (the single-chunk form: one wake time,
-    the earliest arrival over all rows; the reference takes it with an atomic minimum that is only
-    synchronised within a thread block, so its value there can depend on block scheduling)."""
+    lyceanem/electromagnetics/empropagation.py:2910-3170: wake times and source chunks as start_samples
+    describes (the reference takes each wake with an atomic minimum that is only synchronised within a
+    thread block, so its value there can depend on block scheduling; here it is taken first)."""
     del scattering_coefficient, wavelength  # unused by the reference's kernel
     pts = np.asarray(point_informationv2)
     pos = np.stack([pts["px"], pts["py"], pts["pz"]], 1).astype(np.float32)

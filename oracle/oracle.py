@@ -405,14 +405,42 @@ def path_times(full_index, pos, nrm, w, n_src, n_snk, alpha, beta, magnetic=None
     return f * mag[:, None], length / 299792458.0 + delay, pair
 
 
-def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples):
+def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples, map_bytes_limit=1e9):
     """Each row's excitation times its magnitudes, placed at floor((arrival - wake) / (1 / fs))
-    and cut at num_samples (the accumulation of timedomainkernal); returns (map, wake)."""
+    and cut at num_samples (the accumulation of timedomainkernal); returns (map, reported wake).
+    Wake times follow TimeDomainv3 (lyceanem/electromagnetics/empropagation.py:2955-3170), taken
+    before any row is placed: one wake, min(1 s, arrivals), when the float64 map fits map_bytes_limit;
+    else source chunks (np.linspace bounds) whose wake array starts at ones, chunk n updating
+    element 0 of a copy of it (chunk 0 from 1 s, later chunks from chunk 0's result) and storing it
+    as its own; chunks whose wakes differ by a sample or more are shifted by round((wake_n - min) /
+    step) samples (the alignment the reference intends; its slice for the minimum chunk is empty and
+    raises); the reported wake is chunk 0's."""
     S = int(num_samples)
+    step = 1.0 / sampling_freq
     exc = np.asarray(excitation, np.float64).ravel()
     out = np.zeros((n_src, n_snk, S, 3))
-    wake = float(np.min(arrival))
-    t0 = np.floor_divide(np.asarray(arrival) - wake, 1.0 / sampling_freq).astype(np.int64)
+    arrival = np.asarray(arrival, np.float64)
+    src_row = np.asarray(pair)[:, 0]
+    nbytes = float(n_src) * n_snk * S * 3 * 8
+    if np.ceil(nbytes / map_bytes_limit) > 1:
+        bounds = np.linspace(0, n_src, int(np.ceil(nbytes / map_bytes_limit)) + 1).astype(np.int32)
+        wake_times = np.ones(len(bounds) - 1)
+        t0 = np.zeros(len(arrival), np.int64)
+        for n in range(len(bounds) - 1):
+            rows = (src_row >= bounds[n]) & (src_row < bounds[n + 1])
+            d = wake_times.copy()
+            if rows.any():
+                d[0] = min(d[0], float(arrival[rows].min()))
+            t0[rows] = np.floor_divide(arrival[rows] - d[0], step).astype(np.int64)
+            wake_times[n] = d[0]
+        if np.max((wake_times - np.min(wake_times)) / step) >= 1.0:
+            adj = np.round((wake_times - np.min(wake_times)) / step).astype(np.int64)
+            for n in range(len(bounds) - 1):
+                t0[(src_row >= bounds[n]) & (src_row < bounds[n + 1])] += adj[n]
+        wake = float(wake_times[0])
+    else:
+        wake = min(1.0, float(np.min(arrival)))
+        t0 = np.floor_divide(arrival - wake, step).astype(np.int64)
     for r in range(len(t0)):
         k = min(exc.size, S - t0[r])
         if k > 0:

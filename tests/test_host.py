@@ -1,5 +1,6 @@
 """Host-side logic on CPU: scene recipes, chunking, steering weights, sink grids."""
 import numpy as np
+import pytest
 
 from lyceanem_gb300 import scenes
 
@@ -127,3 +128,29 @@ def test_mesh_conversion_records():
 
     assert np.array_equal(mesh_conversion(Structures()), both)
     assert mesh_conversion(object()).shape == (0,)
+
+
+@pytest.mark.parametrize("limit_div,spread", [(1.0, 1e-12), (3.5, 1e-12), (3.5, 3e-9), (7.2, 3e-9)])
+def test_time_map_source_chunks_vs_oracle(limit_div, spread):
+    """Wake times of the time map, single and split into source chunks (TimeDomainv3 splits a float64 map of
+    more than 1e9 bytes; here the limit is lowered to split a small map), against the oracle's loop over the
+    reference's chunk sequence: chunk wakes within one sample (no shift) and chunks whose wakes differ by
+    several samples (shifted into alignment).  Host-side: the map is built from CPU tensors."""
+    import torch
+
+    from lyceanem_gb300.empropagation import time_map
+    from oracle import oracle as O
+    rng = np.random.default_rng(int(limit_div * 10))
+    n_src, n_snk, S, R = 9, 5, 300, 400
+    pair = np.stack([rng.integers(0, n_src, R), rng.integers(0, n_snk, R)], 1).astype(np.int32)
+    # later sources arrive earlier by up to `spread` seconds, so the chunks' wakes differ
+    arrival = 3e-8 + rng.uniform(0, 2e-9, R) - spread * pair[:, 0] / n_src
+    amp = rng.normal(size=(R, 3))
+    exc = np.sin(np.linspace(0, 5 * np.pi, 30))
+    limit = n_src * n_snk * S * 3 * 8 / limit_div
+    fs = 20e9
+    tm, wake = time_map(torch.from_numpy(amp), torch.from_numpy(arrival), torch.from_numpy(pair), n_src, n_snk, exc,
+                        fs, S, map_bytes_limit=limit)
+    otm, owake = O.time_map(amp, arrival, pair, n_src, n_snk, exc, fs, S, map_bytes_limit=limit)
+    assert wake == owake
+    assert np.abs(tm.numpy() - otm).max() <= 1e-12 * np.abs(otm).max()
