@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--batched-cell-scale", type=float, default=0.0,
                     help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
+    ap.add_argument("--traversal", type=int, default=0,
+                    help="grid schedule of the pair stages (0 = automatic; see lyem_pair_stage in include/lyem.h)")
     return ap.parse_args()
 
 
@@ -217,14 +219,15 @@ def run_ours(args, rank, world):
         o_scat = P.spatial_order(scat)  # scatter points are traced in Morton order
         o_snk = P.direction_order(snk, grid.centre)  # sinks in direction order from the scene
         out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct,
-                           snk_order=o_snk).sink
+                           snk_order=o_snk, traversal=args.traversal).sink
         e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=cnt_all,
-                           snk_visible=vis_scat_in, snk_order=o_scat).sink
+                           snk_visible=vis_scat_in, snk_order=o_scat, traversal=args.traversal).sink
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
         P.pair_stage(scat, e_p, snk, snk_n, beta=beta, grid=grid, src_W=e_p, sink_out=out, accumulate=True,
-                     counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat, snk_order=o_snk)
+                     counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat, snk_order=o_snk,
+                     traversal=args.traversal)
         b.record()
         if mark:
             ev.setdefault("s2_list", []).append((a, b))

@@ -374,9 +374,15 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     p.snk_visible = d_snk_visible;
     p.src_order = d_src_order;
     p.snk_order = d_snk_order;
-    if (traversal < 0 || traversal > 36) return LYEM_ERR_INVALID;
+    const bool two_phase = (traversal >= 101 && traversal <= 164) || (traversal >= 201 && traversal <= 264);
+    if ((traversal < 0 || traversal > 36) && !two_phase) return LYEM_ERR_INVALID;
     static const int kCapped[3] = {-10, -12, -16};  // traversal 34, 35, 36
-    p.refill_lanes = traversal == 0 ? -16 : traversal == 1 ? 0 : traversal <= 33 ? traversal - 1 : kCapped[traversal - 34];
+    if (two_phase) {
+        p.refill_lanes = traversal < 200 ? -116 : -112;
+        p.near_dist = (float)(traversal % 100) * (use_grid ? grid_cell : 1.f);
+    } else {
+        p.refill_lanes = traversal == 0 ? -16 : traversal == 1 ? 0 : traversal <= 33 ? traversal - 1 : kCapped[traversal - 34];
+    }
     if (d_mask_bits && d_snk_order)  // permuted sinks set their mask bits one by one
         LYEM_CK(cudaMemsetAsync(d_mask_bits, 0, sizeof(uint32_t) * (size_t)n_src * (size_t)p.mask_words, s));
     LYEM_CK(launch_pair_stage(p, cull, s));

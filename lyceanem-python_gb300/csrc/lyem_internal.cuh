@@ -54,7 +54,9 @@ struct StageParams {
     int src_chunk;
     long long chunk_base;
     int refill_lanes;  // grid stage schedule: 0 = lockstep, k > 0 = batched refill once k lanes are idle,
-                       // -10 / -12 / -16 = lockstep with registers capped for that many blocks per SM
+                       // -10 / -12 / -16 = lockstep with registers capped for that many blocks per SM,
+                       // -116 / -112 = two phases split at near_dist, capped for 16 / 12 blocks per SM
+    float near_dist;   // two-phase schedule: ray parameter (m) where phase 1 hands open rays to phase 2
     // outputs
     float* partial;              // [n_chunks, n_snk, 6]
     float* pair_out;             // [n_src, n_snk, 6] or nullptr

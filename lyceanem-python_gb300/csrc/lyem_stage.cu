@@ -350,9 +350,20 @@ constexpr int kRefill = 1;
 constexpr int kLockstep10 = 2;
 constexpr int kLockstep12 = 3;
 constexpr int kLockstep16 = 4;
+// Two phases (registers capped for 16 or 12 blocks per SM).  Phase 1 runs the
+// lockstep schedule but walks each ray only up to parameter near_dist (most
+// blocked rays end near their origin: the own-surface triangle, local
+// clutter); the rays still open there are appended, source-major, to a queue
+// of the warp in shared memory (ballot + prefix count).  Phase 2 takes them 32
+// at a time, each lane one ray (the sink coordinates come from the owning lane
+// by shuffle), and walks them from near_dist to their end, so the lanes of a
+// warp hold live rays of one or two sources instead of idling behind the
+// longest ray of each source.
+constexpr int kTwoPhase16 = 5;
+constexpr int kTwoPhase12 = 6;
 
 template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, int MODE>
-__global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == kLockstep12 ? 12 : MODE == kLockstep16 ? 16 : 1) grid_stage_kernel(const StageParams p) {
+__global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == kLockstep12 || MODE == kTwoPhase12) ? 12 : (MODE == kLockstep16 || MODE == kTwoPhase16) ? 16 : 1) grid_stage_kernel(const StageParams p) {
     const int tid = threadIdx.x;
     const long long ms = (long long)blockIdx.x * kThreads + tid;
     const bool m_ok = ms < p.n_snk;
@@ -369,7 +380,81 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : MODE == k
     }
     unsigned long long blocked = 0, tests = 0;
     Walk w;
-    if (MODE != kRefill) {
+    if (MODE == kTwoPhase16 || MODE == kTwoPhase12) {
+        __shared__ int s_hint[kGridMaxChunk];
+        __shared__ unsigned long long s_blk[kThreads / 32][32];
+        extern __shared__ unsigned short s_queue[];  // per warp: src_chunk x 32 entries (source << 5 | lane)
+        const int lane = tid & 31, warp = tid >> 5;
+        unsigned short* queue = s_queue + (size_t)warp * p.src_chunk * 32;
+        s_blk[warp][lane] = 0ull;
+        for (int s = warp; s < nsrc; s += kThreads / 32) {
+            const float* so = p.src_pos + 3 * src_index(s);
+            const int h = warp_nearest_ref(p, so[0], so[1], so[2]);
+            if (lane == 0) s_hint[s] = h;
+        }
+        __syncthreads();
+        const float near = p.near_dist;
+        const unsigned full = 0xffffffffu;
+        int count = 0;  // the same in every lane of the warp
+        for (int s = 0; s < nsrc; ++s) {
+            const long long n = src_index(s);
+            bool far = false;
+            if (m_ok && !(p.skip_diag && n == m)) {
+                const float* so = p.src_pos + 3 * n;
+                walk_ray<CULL>(w, so[0], so[1], so[2], ex, ey, ez);
+                const int hint = s_hint[s];
+                bool hit = false;
+                if (hint >= 0) {
+                    ++tests;
+                    hit = walk_test_ref<CULL>(p, w, hint);
+                }
+                if (!hit && walk_setup(p, w)) {
+                    while (true) {
+                        while (w.q < w.q1) {
+                            ++tests;
+                            if (walk_test<CULL>(p, w)) { hit = true; break; }
+                        }
+                        if (hit) break;
+                        const int st = walk_step_until(p, w, near, &g_device_error);
+                        if (st != 1) {
+                            far = st == 2;
+                            break;
+                        }
+                    }
+                }
+                if (hit) blocked |= 1ull << s;
+            }
+            const unsigned fb = __ballot_sync(full, far);
+            if (far) queue[count + __popc(fb & ((1u << lane) - 1u))] = (unsigned short)((s << 5) | lane);
+            count += __popc(fb);
+        }
+        __syncwarp();
+        for (int base = 0; base < count; base += 32) {
+            const int i = base + lane;
+            const bool has = i < count;
+            const unsigned e = has ? queue[i] : 0u;
+            const int owner = (int)(e & 31u), s = (int)(e >> 5);
+            const float qx = __shfl_sync(full, ex, owner), qy = __shfl_sync(full, ey, owner),
+                        qz = __shfl_sync(full, ez, owner);
+            if (has) {
+                const float* so = p.src_pos + 3 * src_index(s);
+                walk_ray<CULL>(w, so[0], so[1], so[2], qx, qy, qz);
+                bool hit = false;
+                if (walk_setup_from(p, w, near)) {
+                    while (!hit) {
+                        while (w.q < w.q1) {
+                            ++tests;
+                            if (walk_test<CULL>(p, w)) { hit = true; break; }
+                        }
+                        if (hit || !walk_step(p, w, &g_device_error)) break;
+                    }
+                }
+                if (hit) atomicOr(&s_blk[warp][owner], 1ull << s);
+            }
+        }
+        __syncwarp();
+        blocked |= s_blk[warp][lane];
+    } else if (MODE != kRefill) {
         // per source of the chunk, the triangle nearest to it (one warp per source):
         // tried first by every ray from that source
         __shared__ int s_hint[kGridMaxChunk];
@@ -470,7 +555,13 @@ static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
         p.chunk_base = base;
         dim3 grid(tiles, (unsigned)(chunks - base < 65535 ? chunks - base : 65535));
         if (p.cell_start) {
-            if (p.refill_lanes == -16)
+            if (p.refill_lanes == -116 || p.refill_lanes == -112) {
+                const size_t qbytes = (size_t)(kThreads / 32) * p.src_chunk * 32 * sizeof(unsigned short);
+                if (p.refill_lanes == -116)
+                    grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase16><<<grid, kThreads, qbytes, stream>>>(p);
+                else
+                    grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase12><<<grid, kThreads, qbytes, stream>>>(p);
+            } else if (p.refill_lanes == -16)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);
             else if (p.refill_lanes == -12)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep12><<<grid, kThreads, 0, stream>>>(p);

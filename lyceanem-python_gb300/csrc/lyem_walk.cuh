@@ -174,6 +174,75 @@ __device__ __forceinline__ bool walk_test_ref(const GP& p, const Walk& w, int q)
     return hit_full<CULL>(w.r, w.ox, w.oy, w.oz, __ldg(t), __ldg(t + 1), __ldg(t + 2), p.eps);
 }
 
+// Enters the grid along the segment set by walk_ray at parameter `from` (a point
+// inside the segment that an earlier partial walk stopped at); false if the rest
+// of the segment misses the grid box.  The cell of the restart point is walked
+// again, so every cell the segment crosses beyond `from` is visited.
+template <class GP>
+__device__ __forceinline__ bool walk_setup_from(const GP& p, Walk& w, float from) {
+    const float ox = w.ox, oy = w.oy, oz = w.oz;
+    float t0 = from;
+    w.t1 = w.r.len;
+    bool miss = false;
+#define LYEM_SLAB(D, O, G0, G1, INV)                       \
+    if (D == 0.f) {                                        \
+        INV = 0.f;                                         \
+        if (O < G0 || O > G1) miss = true;                 \
+    } else {                                               \
+        INV = 1.0f / D;                                    \
+        float ta = (G0 - O) * INV, tb = (G1 - O) * INV;    \
+        t0 = fmaxf(t0, fminf(ta, tb));                     \
+        w.t1 = fminf(w.t1, fmaxf(ta, tb));                 \
+    }
+    LYEM_SLAB(w.r.dx, ox, p.g0[0], p.g1[0], w.ix)
+    LYEM_SLAB(w.r.dy, oy, p.g0[1], p.g1[1], w.iy)
+    LYEM_SLAB(w.r.dz, oz, p.g0[2], p.g1[2], w.iz)
+#undef LYEM_SLAB
+    if (miss || !(t0 <= w.t1)) return false;
+    w.cx = min(max((int)floorf((ox + t0 * w.r.dx - p.g0[0]) * p.inv_cell), 0), p.dims[0] - 1);
+    w.cy = min(max((int)floorf((oy + t0 * w.r.dy - p.g0[1]) * p.inv_cell), 0), p.dims[1] - 1);
+    w.cz = min(max((int)floorf((oz + t0 * w.r.dz - p.g0[2]) * p.inv_cell), 0), p.dims[2] - 1);
+    w.guard = p.dims[0] + p.dims[1] + p.dims[2] + 2;
+    walk_enter(p, w, (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx);
+    return true;
+}
+
+// Crosses the nearest cell boundary unless the crossing lies at or beyond
+// parameter `stop`: 0 = the segment or the grid ends there, 1 = the next cell
+// was entered, 2 = stopped before a crossing at or beyond `stop`.
+template <class GP>
+__device__ __forceinline__ int walk_step_until(const GP& p, Walk& w, float stop, unsigned int* err) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float cell = p.cell;
+    const float tx = w.r.dx > 0.f ? (p.g0[0] + (float)(w.cx + 1) * cell - w.ox) * w.ix
+                                  : (w.r.dx < 0.f ? (p.g0[0] + (float)w.cx * cell - w.ox) * w.ix : kInf);
+    const float ty = w.r.dy > 0.f ? (p.g0[1] + (float)(w.cy + 1) * cell - w.oy) * w.iy
+                                  : (w.r.dy < 0.f ? (p.g0[1] + (float)w.cy * cell - w.oy) * w.iy : kInf);
+    const float tz = w.r.dz > 0.f ? (p.g0[2] + (float)(w.cz + 1) * cell - w.oz) * w.iz
+                                  : (w.r.dz < 0.f ? (p.g0[2] + (float)w.cz * cell - w.oz) * w.iz : kInf);
+    const float tc = fminf(tx, fminf(ty, tz));
+    if (tc > w.t1) return 0;
+    if (tc >= stop) return 2;
+    bool done;
+    if (tx <= ty && tx <= tz) {
+        w.cx += w.r.dx > 0.f ? 1 : -1;
+        done = w.cx < 0 || w.cx >= p.dims[0];
+    } else if (ty <= tz) {
+        w.cy += w.r.dy > 0.f ? 1 : -1;
+        done = w.cy < 0 || w.cy >= p.dims[1];
+    } else {
+        w.cz += w.r.dz > 0.f ? 1 : -1;
+        done = w.cz < 0 || w.cz >= p.dims[2];
+    }
+    if (--w.guard < 0) {  // a monotone walk visits at most dims[0] + dims[1] + dims[2] cells
+        if (err) atomicOr(err, 2u);
+        done = true;
+    }
+    if (done) return 0;
+    walk_enter(p, w, (w.cz * p.dims[1] + w.cy) * p.dims[0] + w.cx);
+    return 1;
+}
+
 // Crosses the nearest cell boundary; false when the segment or the grid ends there.
 template <class GP>
 __device__ __forceinline__ bool walk_step(const GP& p, Walk& w, unsigned int* err) {

@@ -284,6 +284,33 @@ def test_bounce_config_full_geometry_slice():
     assert rel_err(field.cpu().numpy(), ref) < FIELD_TOL
 
 
+@pytest.mark.parametrize("traversal", [36, 1, 102, 104, 203])
+def test_grid_schedules_bit_identical_full_geometry(traversal):
+    """Every grid schedule (lockstep capped and uncapped; two phases split at 2, 4 and 3 cells) gives the
+    oracle's masks and the same sink field on the full 28 GHz geometry (slice of sinks and scatter points,
+    the benchmarked processing orders), for the array-to-sink and scatter-to-sink stages."""
+    from lyceanem_gb300 import scenes
+    P = _P()
+    s = scenes.bounce_scene()
+    beta = 2 * np.pi / s.wavelength
+    snk, snk_n = s.snk[::97], s.snk_n[::97]
+    scat, scat_n = s.scat[::131], s.scat_n[::131]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    grid = P.UniformGrid(P.pack_triangles(t(s.verts), t(s.faces)), cell=s.cell)
+    yk, ykn, pk = t(snk), t(snk_n), t(scat)
+    o_snk, o_scat = P.direction_order(yk, grid.centre), P.spatial_order(pk)
+    og = O.Grid(O.pack_triangles(s.verts, s.faces), s.cell)
+    W = torch.ones((pk.shape[0], 3), dtype=torch.complex64, device="cuda")
+    for a, b, bn, kw in ((s.src, snk, snk_n, dict(snk_order=o_snk)),
+                         (scat, snk, snk_n, dict(src_order=o_scat, snk_order=o_snk, src_W=W))):
+        E = np.ones((a.shape[0], 3), np.complex64)
+        ref = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=36, **kw)
+        r = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=traversal, **kw)
+        assert np.array_equal(r.mask().cpu().numpy(), og.mask(a, b))
+        assert torch.equal(r.sink, ref.sink)
+    _no_device_errors()
+
+
 def test_em_dropin_functions():
     """The four lyceanem.em functions against the oracle network."""
     from lyceanem_gb300 import em
