@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--batched-cell-scale", type=float, default=0.0,
                     help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
+    ap.add_argument("--sweep-case", choices=["full", "small"], default="full",
+                    help="small: the beam-sweep scene on a 4 deg sink grid (4,186 sinks; profiling case)")
     ap.add_argument("--traversal", type=int, default=0,
                     help="grid schedule of the pair stages (0 = automatic; see lyem_pair_stage in include/lyem.h)")
     return ap.parse_args()
@@ -376,7 +378,7 @@ def run_sweep(args, n_check=256, reps=5):
     from lyceanem_gb300 import propagation as P
     from lyceanem_gb300 import scenes
     from oracle import oracle as O
-    s = scenes.sweep_scene()
+    s = scenes.sweep_scene(el_n=46, az_n=91) if args.sweep_case == "small" else scenes.sweep_scene()
     beta = 2 * np.pi / s.wavelength
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
     tris = P.pack_triangles(t(s.verts), t(s.faces))
