@@ -89,6 +89,8 @@ def parse():
     ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
     ap.add_argument("--sweep-case", choices=["full", "small"], default="full",
                     help="small: the beam-sweep scene on a 4 deg sink grid (4,186 sinks; profiling case)")
+    ap.add_argument("--src-chunk", type=int, default=0,
+                    help="sources per thread block of the pair stages (0 = automatic)")
     ap.add_argument("--traversal", type=int, default=0,
                     help="grid schedule of the pair stages (0 = automatic; see lyem_pair_stage in include/lyem.h)")
     return ap.parse_args()
@@ -221,15 +223,16 @@ def run_ours(args, rank, world):
         o_scat = P.spatial_order(scat)  # scatter points are traced in Morton order
         o_snk = P.direction_order(snk, grid.centre)  # sinks in direction order from the scene
         out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=cnt_all, snk_visible=vis_direct,
-                           snk_order=o_snk, traversal=args.traversal).sink
+                           snk_order=o_snk, traversal=args.traversal, src_chunk=args.src_chunk).sink
         e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=cnt_all,
-                           snk_visible=vis_scat_in, snk_order=o_scat, traversal=args.traversal).sink
+                           snk_visible=vis_scat_in, snk_order=o_scat, traversal=args.traversal,
+                           src_chunk=args.src_chunk).sink
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
         P.pair_stage(scat, e_p, snk, snk_n, beta=beta, grid=grid, src_W=e_p, sink_out=out, accumulate=True,
                      counters=cnt_s2, src_visible=vis_scat_out, src_order=o_scat, snk_order=o_snk,
-                     traversal=args.traversal)
+                     traversal=args.traversal, src_chunk=args.src_chunk)
         b.record()
         if mark:
             ev.setdefault("s2_list", []).append((a, b))
@@ -403,8 +406,8 @@ def run_sweep(args, n_check=256, reps=5):
     peak, peak_src = measured_peak("bf16_tflops")
     res["tensor_issued_flops"] = issued
     outs = {}
-    for name, mode, k_tile in (("fp32", "fp32", 64), ("bf16x3g", "bf16x3g", 64), ("fp16x3g", "fp16x3g", 64),
-                               ("bf16x3g_k32", "bf16x3g", 32)):
+    for name, mode, k_tile in (("fp32", "fp32", 32), ("bf16x3g", "bf16x3g", 32), ("fp16x3g", "fp16x3g", 32),
+                               ("bf16x3g_k64", "bf16x3g", 64)):
         BS.set_k_tile(k_tile)
         sw = BS.BeamSweep(G, mode)
         out = sw.run(W)
@@ -426,10 +429,10 @@ def run_sweep(args, n_check=256, reps=5):
             res[name]["tensor_frac"] = issued / (ms * 1e-3) / 1e12 / peak
         del sw, out
         torch.cuda.empty_cache()
-    BS.set_k_tile(64)
+    BS.set_k_tile(32)
     st, flags = P.device_errors()
     res["device_errors"] = [int(st), int(flags)]
-    res["roofline"] = {"bound": "tensor", "kernel": "sweep_tc_kernel (bf16x3g, k-tile 64)",
+    res["roofline"] = {"bound": "tensor", "kernel": "sweep_tc_kernel (bf16x3g, k-tile 32)",
                        "achieved": res["bf16x3g"]["tensor_tflops_issued"], "peak": peak, "unit": "TFLOP/s",
                        "frac": res["bf16x3g"]["tensor_frac"], "peak_source": peak_src,
                        "note": "achieved = issued tensor flops (whole tiles, 9 real products per complex product) / "

@@ -258,8 +258,8 @@ LYEM_API size_t lyem_sweep_workspace_bytes(int64_t ld, int64_t n_beams, int32_t 
 LYEM_API int lyem_sweep_run_ws(const void *d_network, int64_t n_src, int64_t n_snk, int64_t ld, const float *d_W,
                                const void *d_B, int64_t n_beams, int32_t mode, float *d_out, int64_t ldc, void *d_ws,
                                size_t ws_bytes, void *stream);
-/* Sources per pipeline stage of the tensor-core kernel (process-wide): 64
- * (default; 128-byte swizzled rows, 2 stages) or 32 (64-byte rows, 4 stages).
+/* Sources per pipeline stage of the tensor-core kernel (process-wide): 32
+ * (default; 64-byte swizzled rows, 4 stages) or 64 (128-byte rows, 2 stages).
  * Results are the same; only the speed differs.  No counterpart in the reference. */
 LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile);
 

@@ -23,7 +23,7 @@ MODES = {"fp32": 0, "bf16x3g": 3, "fp16x3g": 4}
 
 
 def set_k_tile(k_tile):
-    """Sources per pipeline stage of the tensor-core kernel: 64 (default) or 32."""
+    """Sources per pipeline stage of the tensor-core kernel: 32 (default) or 64."""
     check(lib.lyem_sweep_set_k_tile(int(k_tile)), "sweep_set_k_tile")
 
 

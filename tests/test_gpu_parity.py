@@ -563,7 +563,7 @@ def test_beam_sweep_tensor_core_shapes(k_tile, n_src, n_snk, n_beams):
             # no entry is left unwritten (a stale tile would show as a large per-entry error)
             assert np.abs(E - ref).max() < 1e-3 * np.abs(ref).max(), mode
     finally:
-        BS.set_k_tile(64)
+        BS.set_k_tile(32)
 
 
 @pytest.mark.parametrize("scale", [1e-8, 1e-4, 1e4])
