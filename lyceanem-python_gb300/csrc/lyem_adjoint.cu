@@ -14,9 +14,12 @@
 //   grad y_m =  Re( sum_n conj(a_n) J(n,m; e_n, g_m) + sum_p J(p,m; w_p, conj(w_p) (.) g_m) )
 // with Z_p = sum_m conj(L_pm) [ conj(P w_p) (.) g_m + P (conj(w_p) (.) g_m) ] and
 // J_j(s,t; e, Y) = sum_c conj(d G_c / d r_j) Y_c for G = F(r) (n_t . d) P(d) e,
-// r = t - s, evaluated analytically.  The phase beta*r is reduced in FP64 as
-// in the forward kernels; nothing of size N x M is stored (the N x M masks are
-// bits).  Each kernel assigns one "owner" point per thread and a chunk of
+// r = t - s, evaluated analytically.  The phase beta*r is recomputed per pair
+// in float-float (ff_length, ff_phase: r to about 1e-14 relative, the reduced
+// phase to a few 1e-7 rad, as the forward's FP64 reduction rounded to FP32);
+// FP64 would bound these kernels (86 % FP64-pipe activity on the
+// differentiation scene).  Nothing of size N x M is stored (the N x M masks
+// are bits).  Each kernel assigns one "owner" point per thread and a chunk of
 // partners per block row; chunk partial sums are reduced in FP64.
 #include <cuda_runtime.h>
 
@@ -45,10 +48,11 @@ struct PairGeo {
 
 // Geometry and radial factors of the ray s -> t (normal n at t).
 __device__ __forceinline__ PairGeo pair_geo(float ox, float oy, float oz, float tx, float ty, float tz, float nx,
-                                            float ny, float nz, float alpha, float beta_f, double beta_d) {
+                                            float ny, float nz, float alpha, float beta_f, float beta_lo) {
     Ray ray = make_ray(ox, oy, oz, tx, ty, tz);
-    double rl = path_length_fp64(ox, oy, oz, tx, ty, tz, ray.len);
-    float ph = reduced_phase(beta_d, rl);
+    float rh, rl;
+    ff_length(ox, oy, oz, tx, ty, tz, rh, rl);
+    const float ph = ff_phase(beta_f, beta_lo, rh, rl);
     float sn, cs;
     sincosf(ph, &sn, &cs);
     const float r = ray.len, ir = 1.0f / r;
@@ -130,8 +134,7 @@ struct AdjParams {
     const unsigned* mask0;  // [N, ceil(M/32)]
     const unsigned* mask1;  // [N, ceil(P/32)]
     const unsigned* mask2;  // [P, ceil(M/32)]
-    float alpha, beta_f;
-    double beta_d;
+    float alpha, beta_f, beta_lo;  // beta = beta_f + beta_lo (float-float)
     float* partial;
 };
 
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_scatter_kernel(const AdjP
             if (!mask_bit(a.mask2, wM, p, m)) continue;
             const PairGeo g = pair_geo(ox, oy, oz, a.snk_pos[3 * m], a.snk_pos[3 * m + 1], a.snk_pos[3 * m + 2],
                                        a.snk_nrm[3 * m], a.snk_nrm[3 * m + 1], a.snk_nrm[3 * m + 2], a.alpha,
-                                       a.beta_f, a.beta_d);
+                                       a.beta_f, a.beta_lo);
             cpx gm[3], y[3], q[3], qy[3], ed, yd;
             load3(a.grad_E, m, gm);
             project(g, w, q, &ed);
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_source_kernel(const AdjPa
             const float* tn = is_snk ? a.snk_nrm : a.scat_nrm;
             const float nx = tn[3 * t], ny = tn[3 * t + 1], nz = tn[3 * t + 2];
             const PairGeo g = pair_geo(ox, oy, oz, tp[3 * t], tp[3 * t + 1], tp[3 * t + 2], nx, ny, nz, a.alpha,
-                                       a.beta_f, a.beta_d);
+                                       a.beta_f, a.beta_lo);
             cpx Y[3], q[3], ed, jj[3];
             load3(is_snk ? a.grad_E : a.scat_z, t, Y);
             project(g, e, q, &ed);
@@ -224,7 +227,7 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_sink_kernel(const AdjPara
             if (!mask_bit(is_src ? a.mask0 : a.mask2, wM, s, m)) continue;
             const float* sp = is_src ? a.src_pos : a.scat_pos;
             const PairGeo g = pair_geo(sp[3 * s], sp[3 * s + 1], sp[3 * s + 2], tx, ty, tz, nx, ny, nz, a.alpha,
-                                       a.beta_f, a.beta_d);
+                                       a.beta_f, a.beta_lo);
             cpx e[3], Y[3], J[3];
             if (is_src) {
                 load3(a.src_pol, s, e);
@@ -306,7 +309,7 @@ LYEM_API int lyem_adjoint(const float* d_src_pos, const float* d_src_pol, const 
     a.scat_pos = d_scat_pos; a.scat_nrm = d_scat_nrm; a.scat_w = d_scat_w; a.scat_z = d_scat_z; a.P = n_scat;
     a.snk_pos = d_snk_pos; a.snk_nrm = d_snk_nrm; a.grad_E = d_grad_E; a.M = n_snk;
     a.mask0 = d_mask0; a.mask1 = d_mask1; a.mask2 = d_mask2;
-    a.alpha = (float)alpha; a.beta_f = (float)beta; a.beta_d = beta;
+    a.alpha = (float)alpha; a.beta_f = (float)beta; a.beta_lo = (float)(beta - (double)a.beta_f);
     a.partial = static_cast<float*>(d_ws);
     if (n_scat > 0) {
         dim3 g((unsigned)((n_scat + kAdjThreads - 1) / kAdjThreads), (unsigned)chunks_of(n_snk));

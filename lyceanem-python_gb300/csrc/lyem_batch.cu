@@ -110,53 +110,6 @@ struct BatchParams {
     float* field;                  // [n_scenes][n_freq][n_snk][6] output
 };
 
-// ---------------------------------------------------------------- float-float
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// |e - o| as rh + rl.  The coordinate differences are exact as (h, l) pairs,
-// the squares exact as (p, q) pairs; the neglected l*l terms are below
-// 2^-46 of r^2, and one Newton correction of the FP32 square root (whose
-// residual fma(-rh, rh, s) is exact) carries the float-float precision.
-__device__ __forceinline__ void ff_length(float ox, float oy, float oz, float ex, float ey, float ez, float& rh,
-                                          float& rl) {
-    float hx, lx, hy, ly, hz, lz;
-    two_sum(ex, -ox, hx, lx);
-    two_sum(ey, -oy, hy, ly);
-    two_sum(ez, -oz, hz, lz);
-    const float px = __fmul_rn(hx, hx), qx = __fmaf_rn(hx, hx, -px);
-    const float py = __fmul_rn(hy, hy), qy = __fmaf_rn(hy, hy, -py);
-    const float pz = __fmul_rn(hz, hz), qz = __fmaf_rn(hz, hz, -pz);
-    float s1, e1, s2, e2;
-    two_sum(px, py, s1, e1);
-    two_sum(s1, pz, s2, e2);
-    const float cross = __fmaf_rn(hx, lx, __fmaf_rn(hy, ly, __fmul_rn(hz, lz)));
-    const float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(qx, qy), __fmaf_rn(2.f, cross, qz)));
-    rh = __fsqrt_rn(s2);
-    rl = rh > 0.f ? __fmul_rn(__fadd_rn(__fmaf_rn(-rh, rh, s2), lo), __fmul_rn(0.5f, __frcp_rn(rh))) : 0.f;
-}
-
-// (bh + bl) * (rh + rl) reduced to about [-pi, pi].  2 pi = kC1 + kC2 + O(7e-15).
-// x = p - k*kC1 is exact: |x| < 4 and both p and k*kC1 are multiples of
-// 2^-22 there, so it fits 24 bits.  The error is a few 1e-7 rad for any k
-// that the FP32 product admits.
-__device__ __forceinline__ float ff_phase(float bh, float bl, float rh, float rl) {
-    const float kC1 = 6.28318548202514648f;
-    const float kC2 = -1.74845553146951715e-7f;
-    const float kInv = 0.159154936671257019f;
-    const float p = __fmul_rn(bh, rh);
-    const float pe = __fmaf_rn(bh, rh, -p);
-    const float lo = __fadd_rn(pe, __fmaf_rn(bh, rl, __fmul_rn(bl, rh)));
-    const float k = rintf(__fmul_rn(p, kInv));
-    float x = __fmaf_rn(-k, kC1, p);
-    x = __fmaf_rn(-k, kC2, x);
-    return __fadd_rn(x, lo);
-}
-
 // ---------------------------------------------------------------- queue
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {

@@ -113,14 +113,17 @@ void lyem::record_cuda_error(cudaError_t e) { g_last_cuda_error = (int)e; }
 
 // Sources per thread block when the caller passes 0.  Brute force: as many
 // as keep about four waves of blocks in flight (the triangle tiles are
-// re-staged per block).  Grid: 16, measured flat between 8 and 32 on the
-// 28 GHz one-bounce scene, fewer when that would leave under four waves.
+// re-staged per block).  Grid: 16, or 64 for 16,384 sources and more, fewer
+// when that would leave under four waves.  On the 28 GHz one-bounce scene the
+// scatter->sink stage (50,000 sources) measured 539.7 / 536.8 / 537.7 ms at
+// 16 / 32 / 64, and 64 writes a quarter of the per-chunk partial sums of 16;
+// the 1,024-source stages were faster at 16.
 int lyem::auto_src_chunk(long long n_src, long long n_snk, bool grid) {
     const long long tiles = (n_snk + stage_block_threads() - 1) / stage_block_threads();
     const long long waves = (long long)device_sm_count() * 8 * 4;
     long long c;
     if (grid) {
-        c = 16;
+        c = n_src >= 16384 ? 64 : 16;
         while (c > 1 && ((n_src + c - 1) / c) * tiles < waves) c /= 2;
     } else {
         c = (n_src * tiles) / waves;

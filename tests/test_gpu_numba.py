@@ -97,6 +97,24 @@ def test_emgpufreqdomain_vs_oracle(max_scatter):
     _no_device_errors()
 
 
+def test_emgpufreqdomain_many_rows():
+    """The per-path product on a path list of a few hundred thousand rows (32 sources, 400 sinks, 150 scatter
+    points, one bounce) against the FP64 oracle's per-path sum."""
+    from lyceanem_gb300 import raycasting as RC
+    from lyceanem_gb300.empropagation import EMGPUFreqDomain
+    src, snk, snk_n, v, f, E, scat, scat_n = _scene(seed=12, n_src=32, n_snk=400, n_tris=300, n_scat=150)
+    rng = np.random.default_rng(13)
+    pts, pos, nrm, w = _points(src, snk, snk_n, scat, scat_n, E, rng)
+    N, M = src.shape[0], snk.shape[0]
+    idx, _ = RC.workchunkingv2(src, snk, scat, (v, f), 2)
+    assert idx.shape[0] > 100000
+    beta = 2 * np.pi / 0.05
+    S = EMGPUFreqDomain(N, M, idx, pts, 0.05, 0.02, beta)
+    So = O.path_field(idx, pos, nrm, w, N, M, 0.02, beta)
+    assert rel_err(S, So) < FIELD_TOL
+    _no_device_errors()
+
+
 def test_emgpufreqdomain_rejects_bad_rows():
     from lyceanem_gb300._native import LyemError
     from lyceanem_gb300.empropagation import EMGPUFreqDomain
