@@ -406,9 +406,11 @@ def run_sweep(args, n_check=256, reps=5):
     peak, peak_src = measured_peak("bf16_tflops")
     res["tensor_issued_flops"] = issued
     outs = {}
-    for name, mode, k_tile in (("fp32", "fp32", 32), ("bf16x3g", "bf16x3g", 32), ("fp16x3g", "fp16x3g", 32),
-                               ("bf16x3g_k64", "bf16x3g", 64)):
+    for name, mode, k_tile, mc in (("fp32", "fp32", 32, True), ("bf16x3g", "bf16x3g", 32, True),
+                                   ("fp16x3g", "fp16x3g", 32, True), ("bf16x3g_k64", "bf16x3g", 64, True),
+                                   ("bf16x3g_single_cta", "bf16x3g", 32, False)):
         BS.set_k_tile(k_tile)
+        BS.set_multicast(mc)
         sw = BS.BeamSweep(G, mode)
         out = sw.run(W)
         torch.cuda.synchronize()
@@ -425,14 +427,16 @@ def run_sweep(args, n_check=256, reps=5):
         res[name] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12}
         if mode != "fp32":
             res[name]["k_tile"] = k_tile
+            res[name]["multicast_clusters"] = mc
             res[name]["tensor_tflops_issued"] = issued / (ms * 1e-3) / 1e12
             res[name]["tensor_frac"] = issued / (ms * 1e-3) / 1e12 / peak
         del sw, out
         torch.cuda.empty_cache()
     BS.set_k_tile(32)
+    BS.set_multicast(True)
     st, flags = P.device_errors()
     res["device_errors"] = [int(st), int(flags)]
-    res["roofline"] = {"bound": "tensor", "kernel": "sweep_tc_kernel (bf16x3g, k-tile 32)",
+    res["roofline"] = {"bound": "tensor", "kernel": "sweep_tc_kernel (bf16x3g, k-tile 32, multicast clusters of two)",
                        "achieved": res["bf16x3g"]["tensor_tflops_issued"], "peak": peak, "unit": "TFLOP/s",
                        "frac": res["bf16x3g"]["tensor_frac"], "peak_source": peak_src,
                        "note": "achieved = issued tensor flops (whole tiles, 9 real products per complex product) / "

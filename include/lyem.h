@@ -262,6 +262,12 @@ LYEM_API int lyem_sweep_run_ws(const void *d_network, int64_t n_src, int64_t n_s
  * (default; 64-byte swizzled rows, 4 stages) or 64 (128-byte rows, 2 stages).
  * Results are the same; only the speed differs.  No counterpart in the reference. */
 LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile);
+/* 1 (default): the tensor-core kernel runs in clusters of two CTAs on
+ * neighbouring row tiles that share each weight tile, each loading half of it
+ * and multicasting it to both (a third fewer operand bytes requested per SM);
+ * the single-CTA kernel runs instead when no pair can be co-resident.  0: the
+ * single-CTA kernel.  Results are the same.  No counterpart in the reference. */
+LYEM_API int lyem_sweep_set_multicast(int32_t on);
 
 /* --------------------------------------------------------------- adjoint */
 

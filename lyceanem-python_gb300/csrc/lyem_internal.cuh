@@ -99,6 +99,7 @@ int grid_max_src_chunk();
 // [0, 3) of the network, float 0 of the weights) ahead of the K-major planes.
 constexpr size_t kSweepHeaderBytes = 256;
 extern int sweep_tc_k_tile;  // sources per pipeline stage: 32 (64-byte rows, default) or 64 (128-byte rows)
+extern int sweep_tc_multicast;  // 1: clusters of two CTAs sharing the weight tile by multicast; 0: single CTAs
 int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int64_t n_snk, int64_t ld,
                     int64_t n_beams, bool bf16, float* out, int64_t ldc, cudaStream_t stream);
 

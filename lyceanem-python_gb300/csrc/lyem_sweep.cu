@@ -237,6 +237,12 @@ LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile) {
     return LYEM_OK;
 }
 
+LYEM_API int lyem_sweep_set_multicast(int32_t on) {
+    if (on != 0 && on != 1) return LYEM_ERR_INVALID;
+    sweep_tc_multicast = on;
+    return LYEM_OK;
+}
+
 LYEM_API int lyem_sweep_prepare_network(const float* d_pairs, int64_t n_src, int64_t n_snk, int32_t mode, int64_t ld,
                                         void* d_network, void* stream) {
     if (n_src < 0 || n_snk < 0 || !valid_mode(mode) || ld < n_snk || (ld & 7)) return LYEM_ERR_INVALID;

@@ -70,7 +70,12 @@ struct TcParams {
     unsigned int* err;       // device error word
 };
 
-template <int BK, bool BF16>
+// MC: CTAs run in clusters of two that take the row tiles 2 i and 2 i + 1 of one
+// beam tile; each loads half of the shared weight tile and multicasts it to both,
+// so each SM requests 2/3 of the operand bytes of a stage, and a stage is
+// refilled only after both CTAs' MMAs have read it (its empty barrier counts an
+// arrival from each).
+template <int BK, bool BF16, bool MC>
 __global__ void __launch_bounds__(kTcThreads, 1)
     sweep_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const TcParams p) {
@@ -91,7 +96,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < C::kStages; ++s) {
             mbar_init(bar(FULL + s), 1);
-            mbar_init(bar(EMPTY + s), 1);
+            mbar_init(bar(EMPTY + s), MC ? 2 : 1);
         }
         mbar_init(bar(MID_FULL), 1);
         mbar_init(bar(MID_DONE), 4);
@@ -104,10 +109,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     if (warp == 1) tc::tmem_alloc(smem_addr(s_tmem), kTmemCols);
     tc::fence_before();
-    __syncthreads();
+    if (MC)
+        tc::cluster_sync();  // the peer's multicast copies and commits may target these barriers from now on
+    else
+        __syncthreads();
     tc::fence_after();
     const uint32_t tmem = *s_tmem;
-    const int tiles = 3 * p.n_mt * p.n_kt;
+    // tile t -> (component, row tile, beam tile); with MC a cluster takes tile t and the CTA of rank r its row
+    // tile 2 mt + r (past the last row tile for an odd count: zero rows, nothing stored)
+    const int rank = MC ? (int)tc::cluster_ctarank() : 0;
+    const int first = MC ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int step = MC ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+    const int n_rt = MC ? (p.n_mt + 1) / 2 : p.n_mt;
+    const int tiles = 3 * n_rt * p.n_kt;
+    auto decode = [&](int t, int& c, int& mt, int& kt) {
+        c = t / (n_rt * p.n_kt);
+        const int rem = t - c * (n_rt * p.n_kt);
+        mt = rem / p.n_kt;
+        kt = rem - mt * p.n_kt;
+        if (MC) mt = 2 * mt + rank;
+    };
 
     // Bounded wait; gives up early once another role has given up.
     auto wait = [&](uint32_t b, uint32_t parity) -> bool {
@@ -140,9 +161,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             bool issued[C::kStages];
             for (int i = 0; i < C::kStages; ++i) issued[i] = false;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
-                const int c = t / (p.n_mt * p.n_kt), rem = t - c * (p.n_mt * p.n_kt);
-                const int mt = rem / p.n_kt, kt = rem - mt * p.n_kt;
+            for (int t = first; ok && t < tiles; t += step) {
+                int c, mt, kt;
+                decode(t, c, mt, kt);
                 for (int q = 0; ok && q < 3; ++q) {
                     for (int kb = 0; kb < p.n_kb; ++kb) {
                         if (!wait(bar(EMPTY + s), ph ^ 1u)) {
@@ -155,8 +176,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         const int x = kb * BK, pa = (c * 3 + q) * 2;
                         tc::tma_load_3d(st, &tmA, x, mt * kBM, pa, fb);
                         tc::tma_load_3d(st + C::kABytes, &tmA, x, mt * kBM, pa + 1, fb);
-                        tc::tma_load_3d(st + 2 * C::kABytes, &tmB, x, kt * kBN, 2 * q, fb);
-                        tc::tma_load_3d(st + 2 * C::kABytes + C::kBBytes, &tmB, x, kt * kBN, 2 * q + 1, fb);
+                        if (MC) {  // this CTA's half of the weight rows, into both CTAs
+                            const uint32_t half = (uint32_t)rank * (C::kBBytes / 2);
+                            const int y = kt * kBN + rank * (kBN / 2);
+                            tc::tma_load_3d_mc(st + 2 * C::kABytes + half, &tmB, x, y, 2 * q, fb, 0x3);
+                            tc::tma_load_3d_mc(st + 2 * C::kABytes + C::kBBytes + half, &tmB, x, y, 2 * q + 1, fb,
+                                               0x3);
+                        } else {
+                            tc::tma_load_3d(st + 2 * C::kABytes, &tmB, x, kt * kBN, 2 * q, fb);
+                            tc::tma_load_3d(st + 2 * C::kABytes + C::kBBytes, &tmB, x, kt * kBN, 2 * q + 1, fb);
+                        }
                         issued[s] = true;
                         last_par[s] = ph;
                         if (++s == C::kStages) {
@@ -175,7 +204,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             int s = 0, it = 0;
             uint32_t ph = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < tiles; t += gridDim.x, ++it) {
+            for (int t = first; ok && t < tiles; t += step, ++it) {
                 for (int q = 0; ok && q < 3; ++q) {
                     const uint32_t acc = tmem + (q == 0 ? 0u : (uint32_t)kBN);
                     bool w = true;
@@ -202,11 +231,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                             const uint64_t bh = tc::smem_desc(st + 2 * C::kABytes + off, C::kRowBytes);
                             const uint64_t bl = tc::smem_desc(st + 2 * C::kABytes + C::kBBytes + off, C::kRowBytes);
                             const uint32_t first = (q < 2 && kb == 0 && kk == 0) ? 0u : 1u;
-                            tc::mma_f16(acc, ah, bh, idesc, first);
+                            // hi*hi and hi*lo share A hi: it is read from shared memory once
+                            tc::mma_f16_fill_a(acc, ah, bh, idesc, first);
+                            tc::mma_f16_lastuse_a(acc, ah, bl, idesc, 1u);
                             tc::mma_f16(acc, al, bh, idesc, 1u);
-                            tc::mma_f16(acc, ah, bl, idesc, 1u);
                         }
-                        tc::commit(bar(EMPTY + s));  // the stage is free once these MMAs complete
+                        // the stage is free once these MMAs (and, with MC, the peer's) complete
+                        if (MC)
+                            tc::commit_mc(bar(EMPTY + s), 0x3);
+                        else
+                            tc::commit(bar(EMPTY + s));
                         if (++s == C::kStages) {
                             s = 0;
                             ph ^= 1u;
@@ -234,9 +268,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (lane == 0) tc::mbar_arrive(b);
         };
         int it = 0;
-        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++it) {
-            const int c = t / (p.n_mt * p.n_kt), rem = t - c * (p.n_mt * p.n_kt);
-            const int mt = rem / p.n_kt, kt = rem - mt * p.n_kt;
+        for (int t = first; t < tiles; t += step, ++it) {
+            int c, mt, kt;
+            decode(t, c, mt, kt);
             const long long m = (long long)mt * kBM + quad * 32 + lane;
             const float inv = 1.0f / (p.scale_a[c] * p.scale_w[0]);  // powers of two: exact
             float* out = p.out + (size_t)c * p.n_beams * p.ldc * 2;
@@ -285,7 +319,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
     }
     tc::fence_before();
-    __syncthreads();
+    if (MC)
+        tc::cluster_sync();  // neither CTA leaves while the other may still copy into or arrive on it
+    else
+        __syncthreads();
     if (warp == 1) {
         __syncwarp();  // dealloc is a .sync.aligned warp instruction
         tc::fence_after();
@@ -327,15 +364,43 @@ bool make_map(CUtensorMap* m, const void* base, bool bf16, int k, int rows, int 
                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BK, bool BF16>
-cudaError_t launch_tc(const CUtensorMap& a, const CUtensorMap& b, const TcParams& p, cudaStream_t stream) {
+template <int BK, bool BF16, bool MC>
+cudaError_t launch_tc(const CUtensorMap& a, const CUtensorMap& b, const TcParams& p, cudaStream_t stream,
+                      bool* launched) {
     using C = TcCfg<BK>;
-    auto kern = sweep_tc_kernel<BK, BF16>;
+    auto kern = sweep_tc_kernel<BK, BF16, MC>;
+    *launched = false;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::kSmem);
     if (e != cudaSuccess) return e;
-    const int tiles = 3 * p.n_mt * p.n_kt;
-    const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
-    kern<<<grid, kTcThreads, C::kSmem, stream>>>(a, b, p);
+    const int sms = device_sm_count();
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(kTcThreads);
+    cfg.dynamicSmemBytes = C::kSmem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    if (MC) {
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const int tiles = 3 * ((p.n_mt + 1) / 2) * p.n_kt;
+        cfg.gridDim = dim3(2 * sms);  // the occupancy query needs a grid shape
+        int clusters = 0;
+        e = cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
+        if (e != cudaSuccess || clusters < 1) {
+            (void)cudaGetLastError();
+            return cudaSuccess;  // no co-resident pair: the caller uses the single-CTA kernel
+        }
+        cfg.gridDim = dim3(2 * (unsigned)(tiles < clusters ? tiles : clusters));
+    } else {
+        const int tiles = 3 * p.n_mt * p.n_kt;
+        cfg.gridDim = dim3((unsigned)(tiles < sms ? tiles : sms));
+    }
+    e = cudaLaunchKernelEx(&cfg, kern, a, b, p);
+    if (e != cudaSuccess) return e;
+    *launched = true;
     note_launches(1);
     return cudaGetLastError();
 }
@@ -343,6 +408,7 @@ cudaError_t launch_tc(const CUtensorMap& a, const CUtensorMap& b, const TcParams
 }  // namespace
 
 int sweep_tc_k_tile = 32;
+int sweep_tc_multicast = 1;
 
 int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int64_t n_snk, int64_t ld,
                     int64_t n_beams, bool bf16, float* out, int64_t ldc, cudaStream_t stream) {
@@ -350,9 +416,10 @@ int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int
     const long long kpad = (n_src + 7) / 8 * 8;
     const unsigned char* na = static_cast<const unsigned char*>(network);
     const unsigned char* wb = static_cast<const unsigned char*>(weights);
-    CUtensorMap ma, mb;
+    CUtensorMap ma, mb, mb_half;
     if (!make_map(&ma, na + kSweepHeaderBytes, bf16, (int)n_src, (int)n_snk, 18, kpad, ld, bk, kBM) ||
-        !make_map(&mb, wb + kSweepHeaderBytes, bf16, (int)n_src, (int)n_beams, 6, kpad, n_beams, bk, kBN))
+        !make_map(&mb, wb + kSweepHeaderBytes, bf16, (int)n_src, (int)n_beams, 6, kpad, n_beams, bk, kBN) ||
+        !make_map(&mb_half, wb + kSweepHeaderBytes, bf16, (int)n_src, (int)n_beams, 6, kpad, n_beams, bk, kBN / 2))
         return LYEM_ERR_CUDA;
     TcParams p;
     p.n_src = (int)n_src;
@@ -367,11 +434,24 @@ int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int
     p.scale_w = reinterpret_cast<const float*>(wb);
     p.err = device_error_word();
     if (!p.err) return LYEM_ERR_CUDA;
-    cudaError_t e;
-    if (bk == 64)
-        e = bf16 ? launch_tc<64, true>(ma, mb, p, stream) : launch_tc<64, false>(ma, mb, p, stream);
-    else
-        e = bf16 ? launch_tc<32, true>(ma, mb, p, stream) : launch_tc<32, false>(ma, mb, p, stream);
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    if (sweep_tc_multicast) {  // clusters of two sharing the weight tile; the single-CTA kernel if none fit
+        if (bk == 64)
+            e = bf16 ? launch_tc<64, true, true>(ma, mb_half, p, stream, &done)
+                     : launch_tc<64, false, true>(ma, mb_half, p, stream, &done);
+        else
+            e = bf16 ? launch_tc<32, true, true>(ma, mb_half, p, stream, &done)
+                     : launch_tc<32, false, true>(ma, mb_half, p, stream, &done);
+    }
+    if (e == cudaSuccess && !done) {
+        if (bk == 64)
+            e = bf16 ? launch_tc<64, true, false>(ma, mb, p, stream, &done)
+                     : launch_tc<64, false, false>(ma, mb, p, stream, &done);
+        else
+            e = bf16 ? launch_tc<32, true, false>(ma, mb, p, stream, &done)
+                     : launch_tc<32, false, false>(ma, mb, p, stream, &done);
+    }
     if (e != cudaSuccess) {
         record_cuda_error(e);
         return LYEM_ERR_CUDA;

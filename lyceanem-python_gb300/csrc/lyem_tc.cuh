@@ -40,10 +40,52 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64
         "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
 }
 
+// As mma_f16, keeping A in the tensor core's collector buffer for the next MMA
+// (fill) or taking A from it and releasing it (lastuse): two MMAs in a row on
+// the same A read it from shared memory once.
+__device__ __forceinline__ void mma_f16_fill_a(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                               uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_f16_lastuse_a(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                                  uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate));
+}
+
 // Arrives (once) on the mbarrier when every MMA issued so far by this thread has completed.
 __device__ __forceinline__ void commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
                  : "memory");
+}
+
+// As commit, arriving on the mbarrier at the same shared-memory offset in every CTA of the cluster named by
+// cta_mask (bit i = CTA rank i).
+__device__ __forceinline__ void commit_mc(uint32_t mbar, uint16_t cta_mask) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                     mbar),
+                 "h"(cta_mask)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Barrier of every thread of every CTA of the cluster, ordering the shared-memory writes before it (mbarrier
+// initialisation included) before the other CTAs' accesses after it.
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -128,6 +170,17 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst_smem, const void* tmap,
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
         "[%5];" ::"r"(dst_smem),
         "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(mbar)
+        : "memory");
+}
+
+// As tma_load_3d, writing the box to the same shared-memory offset in every CTA of the cluster named by
+// cta_mask and completing bytes on the mbarrier at the same offset in each of them.
+__device__ __forceinline__ void tma_load_3d_mc(uint32_t dst_smem, const void* tmap, int x, int y, int z, uint32_t mbar,
+                                               uint16_t cta_mask) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, "
+        "{%2, %3, %4}], [%5], %6;" ::"r"(dst_smem),
+        "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(mbar), "h"(cta_mask)
         : "memory");
 }
 

@@ -100,6 +100,7 @@ SIGNATURES = {
     "lyem_sweep_run_ws": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp, _sz, _vp], ctypes.c_int),
     "lyem_sweep_run": ([_vp, _i64, _i64, _i64, _vp, _vp, _i64, _i32, _vp, _i64, _vp], ctypes.c_int),
     "lyem_sweep_set_k_tile": ([_i32], ctypes.c_int),
+    "lyem_sweep_set_multicast": ([_i32], ctypes.c_int),
     "lyem_batch_workspace": ([_scp, _i32, _i64, _i32, _cfgp], _sz),
     "lyem_batch_items": ([_scp, _i32, _i64, _i32, _cfgp, _i64p], ctypes.c_int64),
     "lyem_batch_prepare": ([_scp, _i32, _i64, _f64p, _i32, _cfgp, _vp, _sz, _vp], ctypes.c_int),

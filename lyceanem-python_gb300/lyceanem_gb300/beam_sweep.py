@@ -22,6 +22,12 @@ from ._native import check, lib
 MODES = {"fp32": 0, "bf16x3g": 3, "fp16x3g": 4}
 
 
+def set_multicast(on):
+    """True (default): the tensor-core kernel in clusters of two CTAs sharing each weight tile by multicast;
+    False: single CTAs.  Results are the same."""
+    check(lib.lyem_sweep_set_multicast(int(bool(on))), "sweep_set_multicast")
+
+
 def set_k_tile(k_tile):
     """Sources per pipeline stage of the tensor-core kernel: 32 (default) or 64."""
     check(lib.lyem_sweep_set_k_tile(int(k_tile)), "sweep_set_k_tile")

@@ -545,17 +545,21 @@ def _sweep_vs_fp64(G, W, mode):
     return float(np.linalg.norm(E - ref) / np.linalg.norm(ref)), E, ref
 
 
+@pytest.mark.parametrize("multicast", [True, False])
 @pytest.mark.parametrize("k_tile", [64, 32])
-@pytest.mark.parametrize("n_src,n_snk,n_beams", [(13, 300, 5), (200, 129, 257), (64, 128, 256)])
-def test_beam_sweep_tensor_core_shapes(k_tile, n_src, n_snk, n_beams):
+@pytest.mark.parametrize("n_src,n_snk,n_beams", [(13, 300, 5), (200, 129, 257), (64, 128, 256), (1, 1, 1),
+                                                  (8, 5, 3), (40, 1100, 600)])
+def test_beam_sweep_tensor_core_shapes(multicast, k_tile, n_src, n_snk, n_beams):
     """The tensor-core kernel on ragged sizes (sources not a multiple of 8 or of the k-tile, sinks and
-    beams across tile edges) and on exact tile multiples, both k-tiles, against a complex128 product;
-    every output column and row inside the sizes is written."""
+    beams across tile edges, odd and even counts of sink tiles) and on exact tile multiples, both k-tiles,
+    with and without the two-CTA multicast clusters, against a complex128 product; every output column and
+    row inside the sizes is written."""
     from lyceanem_gb300 import beam_sweep as BS
     g = torch.Generator().manual_seed(n_src * 7 + n_beams)
     G = torch.randn((n_src, n_snk, 3), dtype=torch.complex64, generator=g).cuda()
     W = torch.exp(2j * np.pi * torch.rand((n_beams, n_src), generator=g)).to(torch.complex64).cuda()
     BS.set_k_tile(k_tile)
+    BS.set_multicast(multicast)
     try:
         for mode in ("bf16x3g", "fp16x3g"):
             err, E, ref = _sweep_vs_fp64(G, W, mode)
@@ -564,6 +568,7 @@ def test_beam_sweep_tensor_core_shapes(k_tile, n_src, n_snk, n_beams):
             assert np.abs(E - ref).max() < 1e-3 * np.abs(ref).max(), mode
     finally:
         BS.set_k_tile(32)
+        BS.set_multicast(True)
 
 
 @pytest.mark.parametrize("scale", [1e-8, 1e-4, 1e4])
