@@ -166,7 +166,8 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * trace the same source in lockstep; k in 2..33 = each lane moves on to its
  * next source when its ray ends, new rays being started in batches once k-1
  * lanes of the warp are idle; 34, 35, 36 = lockstep with the registers capped
- * so that 10, 12, 16 blocks fit an SM; 100 + k / 200 + k (k in 1..64) = two
+ * so that 10, 12, 16 blocks fit an SM; 37 = 36 with the largest L1 carve-out
+ * requested for the kernel; 100 + k / 200 + k (k in 1..64) = two
  * phases with the registers capped for 16 / 12 blocks per SM: lockstep up to
  * k grid cells along each ray, then the rays still open are queued per warp
  * and walked to their end 32 at a time; 0 = automatic (currently 36).  Every
@@ -262,11 +263,12 @@ LYEM_API int lyem_sweep_run_ws(const void *d_network, int64_t n_src, int64_t n_s
  * (default; 64-byte swizzled rows, 4 stages) or 64 (128-byte rows, 2 stages).
  * Results are the same; only the speed differs.  No counterpart in the reference. */
 LYEM_API int lyem_sweep_set_k_tile(int32_t k_tile);
-/* 1 (default): the tensor-core kernel runs in clusters of two CTAs on
- * neighbouring row tiles that share each weight tile, each loading half of it
- * and multicasting it to both (a third fewer operand bytes requested per SM);
- * the single-CTA kernel runs instead when no pair can be co-resident.  0: the
- * single-CTA kernel.  Results are the same.  No counterpart in the reference. */
+/* 1: the tensor-core kernel runs in clusters of two CTAs on neighbouring row
+ * tiles that share each weight tile, each loading half of it and multicasting
+ * it to both (a third fewer operand bytes requested per SM); the single-CTA
+ * kernel runs instead when no pair can be co-resident.  0 (default): the
+ * single-CTA kernel, measured as fast or faster.  Results are the same.  No
+ * counterpart in the reference. */
 LYEM_API int lyem_sweep_set_multicast(int32_t on);
 
 /* --------------------------------------------------------------- adjoint */

@@ -57,6 +57,7 @@ struct StageParams {
                        // -10 / -12 / -16 = lockstep with registers capped for that many blocks per SM,
                        // -116 / -112 = two phases split at near_dist, capped for 16 / 12 blocks per SM
     float near_dist;   // two-phase schedule: ray parameter (m) where phase 1 hands open rays to phase 2
+    int l1_max;        // capped lockstep schedule: ask for the largest L1 carve-out (host-side launch setting)
     // outputs
     float* partial;              // [n_chunks, n_snk, 6]
     float* pair_out;             // [n_src, n_snk, 6] or nullptr
@@ -99,7 +100,7 @@ int grid_max_src_chunk();
 // [0, 3) of the network, float 0 of the weights) ahead of the K-major planes.
 constexpr size_t kSweepHeaderBytes = 256;
 extern int sweep_tc_k_tile;  // sources per pipeline stage: 32 (64-byte rows, default) or 64 (128-byte rows)
-extern int sweep_tc_multicast;  // 1: clusters of two CTAs sharing the weight tile by multicast; 0: single CTAs
+extern int sweep_tc_multicast;  // 1: clusters of two CTAs sharing the weight tile by multicast; 0 (default): single CTAs
 int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int64_t n_snk, int64_t ld,
                     int64_t n_beams, bool bf16, float* out, int64_t ldc, cudaStream_t stream);
 

@@ -408,7 +408,7 @@ cudaError_t launch_tc(const CUtensorMap& a, const CUtensorMap& b, const TcParams
 }  // namespace
 
 int sweep_tc_k_tile = 32;
-int sweep_tc_multicast = 1;
+int sweep_tc_multicast = 0;
 
 int launch_sweep_tc(const void* network, const void* weights, int64_t n_src, int64_t n_snk, int64_t ld,
                     int64_t n_beams, bool bf16, float* out, int64_t ldc, cudaStream_t stream) {

@@ -23,8 +23,8 @@ MODES = {"fp32": 0, "bf16x3g": 3, "fp16x3g": 4}
 
 
 def set_multicast(on):
-    """True (default): the tensor-core kernel in clusters of two CTAs sharing each weight tile by multicast;
-    False: single CTAs.  Results are the same."""
+    """True: the tensor-core kernel in clusters of two CTAs sharing each weight tile by multicast; False
+    (default): single CTAs.  Results are the same."""
     check(lib.lyem_sweep_set_multicast(int(bool(on))), "sweep_set_multicast")
 
 

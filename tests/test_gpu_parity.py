@@ -568,7 +568,7 @@ def test_beam_sweep_tensor_core_shapes(multicast, k_tile, n_src, n_snk, n_beams)
             assert np.abs(E - ref).max() < 1e-3 * np.abs(ref).max(), mode
     finally:
         BS.set_k_tile(32)
-        BS.set_multicast(True)
+        BS.set_multicast(False)
 
 
 @pytest.mark.parametrize("scale", [1e-8, 1e-4, 1e4])
