@@ -166,8 +166,7 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * trace the same source in lockstep; k in 2..33 = each lane moves on to its
  * next source when its ray ends, new rays being started in batches once k-1
  * lanes of the warp are idle; 34, 35, 36 = lockstep with the registers capped
- * so that 10, 12, 16 blocks fit an SM; 37 = 36 with the largest L1 carve-out
- * requested for the kernel; 100 + k / 200 + k (k in 1..64) = two
+ * so that 10, 12, 16 blocks fit an SM; 100 + k / 200 + k (k in 1..64) = two
  * phases with the registers capped for 16 / 12 blocks per SM: lockstep up to
  * k grid cells along each ray, then the rays still open are queued per warp
  * and walked to their end 32 at a time; 0 = automatic (currently 36).  Every

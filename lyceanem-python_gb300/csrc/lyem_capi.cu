@@ -378,14 +378,11 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     p.src_order = d_src_order;
     p.snk_order = d_snk_order;
     const bool two_phase = (traversal >= 101 && traversal <= 164) || (traversal >= 201 && traversal <= 264);
-    if ((traversal < 0 || traversal > 37) && !two_phase) return LYEM_ERR_INVALID;
+    if ((traversal < 0 || traversal > 36) && !two_phase) return LYEM_ERR_INVALID;
     static const int kCapped[3] = {-10, -12, -16};  // traversal 34, 35, 36
     if (two_phase) {
         p.refill_lanes = traversal < 200 ? -116 : -112;
         p.near_dist = (float)(traversal % 100) * (use_grid ? grid_cell : 1.f);
-    } else if (traversal == 37) {
-        p.refill_lanes = -16;
-        p.l1_max = 1;
     } else {
         p.refill_lanes = traversal == 0 ? -16 : traversal == 1 ? 0 : traversal <= 33 ? traversal - 1 : kCapped[traversal - 34];
     }

@@ -57,7 +57,6 @@ struct StageParams {
                        // -10 / -12 / -16 = lockstep with registers capped for that many blocks per SM,
                        // -116 / -112 = two phases split at near_dist, capped for 16 / 12 blocks per SM
     float near_dist;   // two-phase schedule: ray parameter (m) where phase 1 hands open rays to phase 2
-    int l1_max;        // capped lockstep schedule: ask for the largest L1 carve-out (host-side launch setting)
     // outputs
     float* partial;              // [n_chunks, n_snk, 6]
     float* pair_out;             // [n_src, n_snk, 6] or nullptr

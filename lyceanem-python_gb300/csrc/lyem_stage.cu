@@ -561,15 +561,9 @@ static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase16><<<grid, kThreads, qbytes, stream>>>(p);
                 else
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase12><<<grid, kThreads, qbytes, stream>>>(p);
-            } else if (p.refill_lanes == -16) {
-                auto kern = grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16>;
-                // the walk uses almost no shared memory; l1_max asks for the largest L1 carve-out
-                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                     p.l1_max ? (int)cudaSharedmemCarveoutMaxL1
-                                                              : (int)cudaSharedmemCarveoutDefault);
-                if (e != cudaSuccess) return e;
-                kern<<<grid, kThreads, 0, stream>>>(p);
-            } else if (p.refill_lanes == -12)
+            } else if (p.refill_lanes == -16)
+                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);
+            else if (p.refill_lanes == -12)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep12><<<grid, kThreads, 0, stream>>>(p);
             else if (p.refill_lanes == -10)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep10><<<grid, kThreads, 0, stream>>>(p);
