@@ -60,10 +60,17 @@ class BeamSweep:
         self.ld = (self.n_snk + 7) // 8 * 8
         nbytes = lib.lyem_sweep_network_bytes(self.n_src, self.ld, self.mode)
         self.operand = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=net.device)
-        check(lib.lyem_sweep_prepare_network(_p(torch.view_as_real(net)), self.n_src, self.n_snk, self.mode, self.ld,
-                                             _p(self.operand), P._stream()), "sweep_prepare_network")
         self._wbuf = None
         self._ws = None
+        self.refresh(net)
+
+    def refresh(self, network):
+        """Rewrites the operand from a network of the same shape (no allocation)."""
+        net = network.contiguous()
+        assert net.dtype == torch.complex64 and tuple(net.shape) == (self.n_src, self.n_snk, 3)
+        check(lib.lyem_sweep_prepare_network(_p(torch.view_as_real(net)), self.n_src, self.n_snk, self.mode, self.ld,
+                                             _p(self.operand), P._stream()), "sweep_prepare_network")
+        return self
 
     def run(self, W, out=None):
         """Sink fields for excitations W complex [K, N]: returns complex64 [3, K, ld] (use .fields())."""
