@@ -140,7 +140,9 @@ def start_samples(arrival, src_of_row, n_src, n_snk, num_samples, sampling_freq,
 
 def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_samples, map_bytes_limit=MAP_BYTES_LIMIT):
     """float64 [n_src, n_snk, num_samples, 3]: each row's excitation, scaled by its magnitudes, starting at
-    the sample start_samples gives it and cut at num_samples; returned with the reported wake time.  Built
+    the sample start_samples gives it and cut at num_samples (timedomainkernal adds the whole excitation
+    where it fits and the part before the end where it does not,
+    lyceanem/electromagnetics/empropagation.py:1509-1578); returned with the reported wake time.  Built
     as an amplitude histogram of start samples per (source, sink) convolved with the excitation (FFT)."""
     dev = amp.device
     S = int(num_samples)
@@ -162,7 +164,7 @@ def time_map(amp, arrival, pair, n_src, n_snk, excitation, sampling_freq, num_sa
 
 def TimeDomainv3(source_num, sink_num, point_informationv2, full_index, scattering_coefficient, wavelength,
                  excitation_signal, sampling_freq, num_samples, alpha, beta):
-    """(time_map float64 [source_num, sink_num, num_samples, 3], wake_times [1]) of
+    """(time_map float64 [source_num, sink_num, num_samples, 3], wake time float64) of
     lyceanem/electromagnetics/empropagation.py:2910-3170: wake times and source chunks as start_samples
     describes (the reference takes each wake with an atomic minimum that is only synchronised within a
     thread block, so its value there can depend on block scheduling; here it is taken first)."""
@@ -180,4 +182,4 @@ def TimeDomainv3(source_num, sink_num, point_informationv2, full_index, scatteri
                                     impedance)
     tm, wake = time_map(amp, arrival, pair, int(source_num), int(sink_num), excitation_signal, sampling_freq,
                         num_samples)
-    return tm.cpu().numpy(), np.array([wake], dtype=np.float64)
+    return tm.cpu().numpy(), np.float64(wake)

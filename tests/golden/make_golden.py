@@ -18,7 +18,18 @@ Fixtures:
                           excitation_function (lyceanem/electromagnetics/emfunctions.py:9-82)
                           and helpers, executed from their source text (the modules
                           themselves import numba and pyvista, absent here)
-Usage: python tests/golden/make_golden.py [reference_root]
+  numba_engine.npz        outputs of the reference's numba engine on small seeded scenes,
+                          executed under numba_sim (a stand-in for numba and cupy that runs the
+                          engine's kernels as Python with numba's typing of constants; see
+                          numba_sim.py for what it reproduces and what it cannot):
+                          workchunkingv2's path index and ray count
+                          (lyceanem/raycasting/rayfunctions.py:2681-2955) for one, two and three
+                          interactions, with and without line of sight; EMGPUFreqDomain
+                          (lyceanem/electromagnetics/empropagation.py:2197-2410) on those paths at
+                          two wavelengths and with magnetic sources; TimeDomainv3 (:2910-3170) on a
+                          one-block path list, with 400 and with 120 samples.  Written last: the
+                          stand-in modules stay installed.
+Usage: python tests/golden/make_golden.py [reference_root] [--only NAME]
 """
 import ast
 import importlib.util
@@ -29,7 +40,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else "/root/reference"
 PKG = os.path.join(REF, "lyceanem")
 
 
@@ -205,9 +216,106 @@ def excitation_cases():
              extra_reference=np.stack([e[3] for e in extra]))
 
 
+def _numba_scene(seed, n_src, n_snk, n_tris, n_scat):
+    """Seeded scene of the numba-engine fixtures: sources below, sinks on a sphere, triangles and
+    scatter points in a box (the recipe of tests/helpers.py random_scene, restated so the
+    fixtures do not depend on it)."""
+    rng = np.random.default_rng(seed)
+    src = np.stack([rng.uniform(-0.5, 0.5, n_src), rng.uniform(-0.5, 0.5, n_src), np.full(n_src, -2.0)],
+                   1).astype(np.float32)
+    d = rng.normal(size=(n_snk, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    snk, snk_n = (4.0 * d).astype(np.float32), (-d).astype(np.float32)
+    c = rng.uniform(-1.0, 1.0, size=(n_tris, 3))
+    verts = (c[:, None, :] + rng.uniform(-0.3, 0.3, size=(n_tris, 3, 3))).reshape(-1, 3).astype(np.float32)
+    faces = np.arange(3 * n_tris, dtype=np.int32).reshape(-1, 3)
+    scat = rng.uniform(-1, 1, (n_scat, 3)).astype(np.float32)
+    scat_n = rng.normal(size=(n_scat, 3)).astype(np.float32)
+    scat_n /= np.linalg.norm(scat_n, axis=1, keepdims=True)
+    w = (rng.normal(size=(n_src + n_snk + n_scat, 3)) + 1j * rng.normal(size=(n_src + n_snk + n_scat, 3)))
+    return dict(src=src, snk=snk, snk_n=snk_n, verts=verts, faces=faces, scat=scat, scat_n=scat_n,
+                w=w.astype(np.complex64))
+
+
+def numba_engine():
+    sys.path.insert(0, HERE)
+    import numba_sim
+    numba_sim.install()
+    sys.path.insert(0, REF)
+    import lyceanem.base_types as BT
+    import lyceanem.electromagnetics.empropagation as EM
+    import lyceanem.raycasting.rayfunctions as RF
+    numba_sim.freeze_float_globals(RF)
+    numba_sim.freeze_float_globals(EM)
+
+    def environment(sc):
+        v, f = sc["verts"], sc["faces"]
+        env = np.empty(f.shape[0], dtype=BT.triangle_t)
+        for k, c in enumerate("xyz"):
+            for j in range(3):
+                env[f"v{j}{c}"] = v[f[:, j], k]
+        return env
+
+    def points(sc, w, magnetic=0):
+        n_src = sc["src"].shape[0]
+        pos = np.concatenate([sc["src"], sc["snk"], sc["scat"]])
+        nrm = np.concatenate([np.tile([[0, 0, 1.0]], (n_src, 1)), sc["snk_n"], sc["scat_n"]]).astype(np.float32)
+        pts = np.zeros(pos.shape[0], dtype=BT.scattering_t.dtype)
+        for k, c in enumerate("xyz"):
+            pts[f"p{c}"], pts[f"n{c}"], pts[f"e{c}"] = pos[:, k], nrm[:, k], w[:, k]
+        pts["Electric"] = True
+        pts["Electric"][:magnetic] = False
+        pts["permittivity"] = 8.8541878176e-12
+        pts["permeability"] = 1.25663706212e-6
+        return pts
+
+    out = {}
+    scenes = {"a": _numba_scene(13, 6, 40, 80, 25), "b": _numba_scene(11, 4, 20, 40, 12),
+              "t": _numba_scene(4, 2, 16, 40, 5)}
+    for name, sc in scenes.items():
+        for k, val in sc.items():
+            out[f"{name}_{k}"] = val
+    # path index: (scene, max_scatter, line of sight)
+    cases = [("a", 1, True), ("a", 2, True), ("a", 2, False), ("b", 3, True), ("b", 3, False), ("t", 2, True)]
+    index = {}
+    for name, ms, los in cases:
+        sc = scenes[name]
+        idx, rays = RF.workchunkingv2(sc["src"], sc["snk"], sc["scat"], environment(sc), ms, line_of_sight=los)
+        key = f"{name}{ms}{'los' if los else 'nolos'}"
+        out[f"index_{key}"], out[f"rays_{key}"] = idx, np.int64(rays)
+        index[key] = idx
+        print("  workchunkingv2", key, idx.shape, rays)
+    # per-path products: (case, wavelength, magnetic sources)
+    alpha = 0.02
+    for key, lam, mag in (("a2los", 0.5, 0), ("a2los", 0.05, 0), ("a2los", 0.5, 3), ("b3los", 0.5, 0)):
+        sc = scenes[key[0]]
+        S = EM.EMGPUFreqDomain(sc["src"].shape[0], sc["snk"].shape[0], index[key], points(sc, sc["w"], mag),
+                               lam, alpha, 2 * np.pi / lam)
+        out[f"field_{key}_{lam}_{mag}"] = S
+        print("  EMGPUFreqDomain", key, lam, mag, S.shape)
+    # time domain on one block of rows (the reference's wake time is block-synchronised only)
+    sc = scenes["t"]
+    idx = index["t2los"]
+    assert idx.shape[0] <= 256, idx.shape
+    rng = np.random.default_rng(2)
+    n_pts = sc["w"].shape[0]
+    wt = (rng.uniform(0.5, 1.5, (n_pts, 3)) + 1j * rng.uniform(0, 2e-9, (n_pts, 3))).astype(np.complex64)
+    exc = np.sin(np.linspace(0, 6 * np.pi, 40)) * np.hanning(40)
+    tm, wake = EM.TimeDomainv3(sc["src"].shape[0], sc["snk"].shape[0], points(sc, wt), idx, 0.25 * np.pi, 0.05, exc,
+                               20e9, 400, alpha, 2 * np.pi / 0.05)
+    out.update(time_w=wt, time_excitation=exc, time_map=tm, time_wake=np.float64(wake))
+    print("  TimeDomainv3", tm.shape, wake)
+    # a short map: the kernel cuts rows whose excitation would run past its end
+    tm, wake = EM.TimeDomainv3(sc["src"].shape[0], sc["snk"].shape[0], points(sc, wt), idx, 0.25 * np.pi, 0.05, exc,
+                               20e9, 120, alpha, 2 * np.pi / 0.05)
+    out.update(time_map_short=tm, time_wake_short=np.float64(wake))
+    print("  TimeDomainv3 short", tm.shape, wake)
+    np.savez_compressed(os.path.join(HERE, "numba_engine.npz"), **out)
+
+
 if __name__ == "__main__":
-    convert_triangles()
-    vector_mapping_cases()
-    tile_structure()
-    excitation_cases()
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    for fn in (convert_triangles, vector_mapping_cases, tile_structure, excitation_cases, numba_engine):
+        if only is None or fn.__name__ == only:
+            fn()
     print("golden fixtures written to", HERE)

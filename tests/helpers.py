@@ -24,3 +24,43 @@ def random_scene(seed, n_src=7, n_snk=45, n_tris=60, box=1.0, src_z=-2.0, snk_r=
     f = np.arange(3 * n_tris, dtype=np.int32).reshape(-1, 3)
     E = (rng.normal(size=(n_src, 3)) + 1j * rng.normal(size=(n_src, 3))).astype(np.complex64)
     return src, snk, snk_n, v, f, E
+
+
+# Numba-engine fixtures (tests/golden/numba_engine.npz, written by make_golden.py from the reference's own
+# numba engine): path-index cases (scene, max_scatter, line of sight) and per-path-product cases
+# (index case, wavelength, magnetic sources, tolerance).  The reference forms path lengths and phases in
+# float32, so at lambda = 0.05 m (k r ~ 250 rad on these ~2 m paths) its own output sits ~2.5e-5 from FP64,
+# ten times closer at 0.5 m; the tolerances say so.
+NUMBA_INDEX_CASES = [("a", 1, True), ("a", 2, True), ("a", 2, False), ("b", 3, True), ("b", 3, False),
+                     ("t", 2, True)]
+NUMBA_FIELD_CASES = [("a2los", 0.5, 0, 1e-5), ("a2los", 0.05, 0, 1e-4), ("a2los", 0.5, 3, 1e-5),
+                     ("b3los", 0.5, 0, 1e-5)]
+NUMBA_ALPHA = 0.02
+
+
+def numba_golden():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "numba_engine.npz"))
+
+
+def numba_index_key(scene, max_scatter, los):
+    return f"{scene}{max_scatter}{'los' if los else 'nolos'}"
+
+
+def numba_golden_scene(d, scene):
+    """(src, snk, scat, verts, faces, pos, nrm, w) of a fixture scene; pos / nrm / w cover
+    [sources, sinks, scatter points] with +z source normals, as the fixtures were made."""
+    g = lambda k: d[f"{scene}_{k}"]  # noqa: E731
+    src, snk, scat = g("src"), g("snk"), g("scat")
+    pos = np.concatenate([src, snk, scat])
+    nrm = np.concatenate([np.tile([[0, 0, 1.0]], (src.shape[0], 1)), g("snk_n"), g("scat_n")]).astype(np.float32)
+    return src, snk, scat, g("verts"), g("faces"), pos, nrm, g("w")
+
+
+def numba_golden_magnetic(n_points, magnetic):
+    """Magnetic flags and impedances of the fixture points (the first `magnetic` sources magnetic)."""
+    mag = np.zeros(n_points, bool)
+    mag[:magnetic] = True
+    imp = np.full(n_points, np.sqrt(np.float32(1.25663706212e-6).astype(np.float64)
+                                    / np.float32(8.8541878176e-12).astype(np.float64)), np.float32)
+    return mag, imp

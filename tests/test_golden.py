@@ -76,3 +76,36 @@ def test_excitation_function_golden():
         desired = d["extra_desired"][i].reshape(1, 3) if name == "no_projection" else d["extra_desired"][i]
         got = excitation_function(_Cloud(d["ap_points"], d["ap_normals"], area), desired, **kws[str(name)])
         np.testing.assert_allclose(got, d["extra_reference"][i], rtol=2e-6, atol=1e-4, err_msg=str(name))
+
+
+def test_numba_engine_golden_oracle():
+    """The oracle's numba-engine restatement against the reference's own numba engine (fixtures made by
+    executing workchunkingv2, EMGPUFreqDomain and TimeDomainv3 from the reference's source,
+    tests/golden/numba_sim.py): path index and ray count row for row, per-path products and the time map
+    within the reference's own float32 rounding."""
+    from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, numba_golden, numba_golden_magnetic,
+                         numba_golden_scene, numba_index_key, rel_err)
+    d = numba_golden()
+    for scene, ms, los in NUMBA_INDEX_CASES:
+        src, snk, scat, v, f, _, _, _ = numba_golden_scene(d, scene)
+        masks = O.numba_masks(src, snk, scat, O.pack_triangles(v, f))
+        idx, rays = O.numba_path_index(src.shape[0], snk.shape[0], scat.shape[0], *masks, ms, line_of_sight=los)
+        key = numba_index_key(scene, ms, los)
+        assert np.array_equal(idx, d[f"index_{key}"]), key
+        assert rays == int(d[f"rays_{key}"]), key
+    for key, lam, mag, tol in NUMBA_FIELD_CASES:
+        src, snk, _, _, _, pos, nrm, w = numba_golden_scene(d, key[0])
+        m, imp = numba_golden_magnetic(pos.shape[0], mag)
+        S = O.path_field(d[f"index_{key}"], pos, nrm, w, src.shape[0], snk.shape[0], NUMBA_ALPHA, 2 * np.pi / lam,
+                         magnetic=m if mag else None, impedance=imp if mag else None)
+        assert rel_err(S, d[f"field_{key}_{lam}_{mag}"]) < tol, (key, lam, mag)
+    src, snk, _, _, _, pos, nrm, _ = numba_golden_scene(d, "t")
+    amp, arr, pair = O.path_times(d["index_t2los"], pos, nrm, d["time_w"], src.shape[0], snk.shape[0], NUMBA_ALPHA,
+                                  2 * np.pi / 0.05)
+    tm, wake = O.time_map(amp, arr, pair, src.shape[0], snk.shape[0], d["time_excitation"], 20e9, 400)
+    assert abs(wake - float(d["time_wake"])) < 1e-14  # seconds: float32 path lengths in the reference
+    assert rel_err(tm, d["time_map"]) < 1e-6
+    tm, wake = O.time_map(amp, arr, pair, src.shape[0], snk.shape[0], d["time_excitation"], 20e9, 120)
+    assert abs(wake - float(d["time_wake_short"])) < 1e-14
+    assert rel_err(tm, d["time_map_short"]) < 1e-6
+

@@ -9,7 +9,8 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import random_scene, rel_err
+from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, numba_golden, numba_golden_scene,
+                     numba_index_key, random_scene, rel_err)
 
 pytestmark = pytest.mark.gpu
 
@@ -156,3 +157,37 @@ def test_calculate_scattering_numba_branch(scattering, los, elements):
         fact = O.numba_sink_field(src, Esrc, snk, snk_n, scat, scat_n, 0.0, beta, masks, scattering, los=los)
         assert rel_err(got, fact) < FIELD_TOL
     _no_device_errors()
+
+
+@pytest.mark.parametrize("scene,max_scatter,los", NUMBA_INDEX_CASES)
+def test_workchunkingv2_reference_golden(scene, max_scatter, los):
+    """workchunkingv2 against the reference's own numba engine (fixture executed from its source):
+    the same rows in the same order, and the same ray count."""
+    from lyceanem_gb300 import raycasting as RC
+    d = numba_golden()
+    src, snk, scat, v, f, _, _, _ = numba_golden_scene(d, scene)
+    idx, rays = RC.workchunkingv2(src, snk, scat, (v, f), max_scatter, line_of_sight=los)
+    key = numba_index_key(scene, max_scatter, los)
+    assert np.array_equal(idx, d[f"index_{key}"])
+    assert rays == int(d[f"rays_{key}"])
+    _no_device_errors()
+
+
+@pytest.mark.parametrize("key,lam,magnetic,tol", NUMBA_FIELD_CASES)
+def test_emgpufreqdomain_reference_golden(key, lam, magnetic, tol):
+    """EMGPUFreqDomain against the reference's own per-path product on the fixture's path list (within the
+    reference's float32 phase rounding, see helpers)."""
+    from lyceanem_gb300.empropagation import EMGPUFreqDomain, scattering_point
+    d = numba_golden()
+    src, snk, _, _, _, pos, nrm, w = numba_golden_scene(d, key[0])
+    pts = np.zeros(pos.shape[0], dtype=scattering_point)
+    for k, c in enumerate("xyz"):
+        pts[f"p{c}"], pts[f"n{c}"], pts[f"e{c}"] = pos[:, k], nrm[:, k], w[:, k]
+    pts["Electric"] = True
+    pts["Electric"][:magnetic] = False
+    pts["permittivity"] = 8.8541878176e-12
+    pts["permeability"] = 1.25663706212e-6
+    S = EMGPUFreqDomain(src.shape[0], snk.shape[0], d[f"index_{key}"], pts, lam, NUMBA_ALPHA, 2 * np.pi / lam)
+    assert rel_err(S, d[f"field_{key}_{lam}_{magnetic}"]) < tol
+    _no_device_errors()
+

@@ -6,7 +6,7 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import random_scene, rel_err
+from helpers import NUMBA_ALPHA, numba_golden, numba_golden_scene, random_scene, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -88,7 +88,34 @@ def test_time_domain_calculate_scattering():
         pts[f"e{c}"] = w[:, j]
     pts["Electric"] = True
     tm, wk = TimeDomainv3(N, M, pts, idx, 0.25 * np.pi, 0.03, exc, fs, S, 0.0, 2 * np.pi / 0.03)
-    assert tm.shape == (N, M, S, 3) and abs(wk[0] - owake) < 1e-15
+    assert tm.shape == (N, M, S, 3) and abs(wk - owake) < 1e-15
     assert rel_err(tm, otm) < 1e-5
     from lyceanem_gb300 import propagation as P
     assert P.device_errors() == (0, 0)
+
+
+def test_timedomainv3_reference_golden():
+    """TimeDomainv3 against the reference's own time kernel on a one-block path list (fixture executed from
+    its source): wake time to the float32 path lengths it forms, time map within 1e-6."""
+    from lyceanem_gb300.empropagation import TimeDomainv3, scattering_point
+    d = numba_golden()
+    src, snk, _, _, _, pos, nrm, _ = numba_golden_scene(d, "t")
+    w = d["time_w"]
+    pts = np.zeros(pos.shape[0], dtype=scattering_point)
+    for k, c in enumerate("xyz"):
+        pts[f"p{c}"], pts[f"n{c}"], pts[f"e{c}"] = pos[:, k], nrm[:, k], w[:, k]
+    pts["Electric"] = True
+    pts["permittivity"] = 8.8541878176e-12
+    pts["permeability"] = 1.25663706212e-6
+    tm, wake = TimeDomainv3(src.shape[0], snk.shape[0], pts, d["index_t2los"], 0.25 * np.pi, 0.05,
+                            d["time_excitation"], 20e9, 400, NUMBA_ALPHA, 2 * np.pi / 0.05)
+    assert abs(wake - float(d["time_wake"])) < 1e-14
+    assert rel_err(tm, d["time_map"]) < 1e-6
+    # 120 samples: rows whose excitation would run past the map are cut at its end
+    tm, wake = TimeDomainv3(src.shape[0], snk.shape[0], pts, d["index_t2los"], 0.25 * np.pi, 0.05,
+                            d["time_excitation"], 20e9, 120, NUMBA_ALPHA, 2 * np.pi / 0.05)
+    assert abs(wake - float(d["time_wake_short"])) < 1e-14
+    assert rel_err(tm, d["time_map_short"]) < 1e-6
+    from lyceanem_gb300 import propagation as P
+    assert P.device_errors() == (0, 0)
+
