@@ -413,10 +413,10 @@ def run_sweep(args, n_check=256, reps=5):
         BS.set_multicast(mc)
         sw = BS.BeamSweep(G, mode)
         torch.cuda.synchronize()
-        x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        x.record()
+        px, py = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        px.record()
         sw.refresh(G)  # the network's operand again: transpose, split, scales (once per network)
-        y.record()
+        py.record()
         out = sw.run(W)
         torch.cuda.synchronize()
         ev = []
@@ -429,7 +429,8 @@ def run_sweep(args, n_check=256, reps=5):
         torch.cuda.synchronize()
         ms = min(x.elapsed_time(y) for x, y in ev)
         outs[name] = sw.fields(out)[torch.from_numpy(pick).cuda()].cpu().numpy()
-        res[name] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12, "prepare_network_ms": x.elapsed_time(y)}
+        res[name] = {"ms": ms, "tflops_algorithmic": flops / (ms * 1e-3) / 1e12,
+                     "prepare_network_ms": px.elapsed_time(py)}
         if mode != "fp32":
             res[name]["k_tile"] = k_tile
             res[name]["multicast_clusters"] = mc
