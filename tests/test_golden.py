@@ -109,3 +109,46 @@ def test_numba_engine_golden_oracle():
     assert abs(wake - float(d["time_wake_short"])) < 1e-14
     assert rel_err(tm, d["time_map_short"]) < 1e-6
 
+
+
+def test_numba_stand_in_typing():
+    """The stand-in that ran the reference's numba engine for the fixtures reproduces numba's typing of
+    constants: a float literal or global promotes float32 to FP64 (F = 1.0 / A), float32 x float32 stays
+    float32, and a kernel's threads run block by block through cuda.syncthreads()."""
+    import sys
+    sys.path.insert(0, GOLD)
+    try:
+        import numba_sim
+    finally:
+        sys.path.remove(GOLD)
+    ns = {"EPS": np.float64(1e-7)}
+    src = ("def f(a, b):\n"
+           "    F = 1.0 / a\n"
+           "    p = a * b\n"
+           "    rejected = -EPS < a < EPS\n"
+           "    return F, p, rejected, 2 * EPS\n")
+    exec(src, ns)
+    import inspect
+    import linecache
+    linecache.cache["<numba_sim_test>"] = (len(src), None, src.splitlines(True), "<numba_sim_test>")
+    ns["f"].__code__ = ns["f"].__code__.replace(co_filename="<numba_sim_test>")
+    assert inspect.getsource(ns["f"]).startswith("def f")
+    g = numba_sim._numba_typed(ns["f"])
+    F, p, rejected, two_eps = g(np.float32(3.0), np.float32(0.1))
+    assert type(F) is np.float64 and F == 1.0 / 3.0
+    assert type(p) is np.float32 and p == np.float32(3.0) * np.float32(0.1)
+    assert not rejected and type(two_eps) is np.float64
+    # barrier: every thread of a block writes before any reads
+    src2 = ("def k(buf, out):\n"
+            "    i = cuda.grid(1)\n"
+            "    buf[i] = i\n"
+            "    cuda.syncthreads()\n"
+            "    out[i] = buf[(i + 1) % 4 + 4 * (i // 4)]\n")
+    ns2 = {"cuda": numba_sim._make_cuda()}
+    exec(src2, ns2)
+    linecache.cache["<numba_sim_test2>"] = (len(src2), None, src2.splitlines(True), "<numba_sim_test2>")
+    ns2["k"].__code__ = ns2["k"].__code__.replace(co_filename="<numba_sim_test2>")
+    kern = numba_sim._Kernel(ns2["k"])
+    buf, out = np.zeros(8, np.int64), np.zeros(8, np.int64)
+    kern[2, 4](buf, out)
+    assert kern.lockstep and out.tolist() == [1, 2, 3, 0, 5, 6, 7, 4]
