@@ -125,3 +125,57 @@ def workchunkingv2(sources, sinks, scattering_points, environment, max_scatter, 
         out.append(torch.cat(rows, 0))
         rays = (s1 - s0) * ((M if line_of_sight else 0) + Pn) + n1.shape[0] * (M + Pn - 1) + n2.shape[0] * M
     return torch.cat(out, 0).to(torch.int32).cpu().numpy().reshape(-1, 4), rays
+
+
+def visiblespace(source_coords, source_normals, environment, vertex_area=0, az_range=None, elev_range=None,
+                 shell_range=0.5):
+    """(visible_patterns float32 [len(elev_range), len(az_range)], sample_shell) of
+    lyceanem/raycasting/rayfunctions.py:316-427: for each point of a shell of radius shell_range
+    (spherical_field, outward normals), the summed projected area of the sources that see it.
+
+    A source n sees shell point m when the numba engine's ray n -> m is unblocked (workchunkingv2 with
+    max_scatter 1, this package's kernels); it contributes area_n |cos angle| where angle is the angle
+    between the ray direction and the source normal (unit vectors, float32 as the reference), and nothing
+    when the angle exceeds pi / 2.  vertex_area: one value per source, or a single value (0, the default,
+    counts every visible pair as 1); NaN areas count as 0 (the reference sets them to 0 in the caller's
+    array and raises for a plain scalar; here the caller's array is left as it is and a scalar is taken
+    as a single value).  The angle's sign, which the reference takes from a 2 x 2 minor, is not formed:
+    only |cos angle| and |angle| are used.  Shell points are in this package's spherical_field order
+    (elevation-major), so the patterns reshape to [elevation, azimuth]; sample_shell.point_data
+    ["Projected_Area"] holds them as a column."""
+    from .geometry import spherical_field
+    if az_range is None:
+        az_range = np.linspace(-180.0, 180.0, 19)
+    if elev_range is None:
+        elev_range = np.linspace(-90.0, 90.0, 19)
+    pts = np.asarray(getattr(source_coords, "points", source_coords), dtype=np.float32).reshape(-1, 3)
+    n_src = pts.shape[0]
+    shell = spherical_field(az_range, elev_range, outward_normals=True, field_radius=shell_range)
+    sinks = np.asarray(shell.points, dtype=np.float32)
+    n_snk = sinks.shape[0]
+    hit_index, _ = workchunkingv2(pts, sinks, np.empty((0, 3), np.float32), environment, 1)
+    src_t = P._points(pts)
+    dev = src_t.device
+    hi = torch.as_tensor(hit_index, device=dev).long().reshape(-1, 2)
+    si, mi = hi[:, 0] - 1, hi[:, 1] - 1 - n_src
+    # calc_dv_norm (lyceanem/utility/math_functions.py:149-156): float32, nothing fused
+    r = P._points(sinks)[mi] - src_t[si]
+    length = torch.sqrt((r[:, 0] * r[:, 0] + r[:, 1] * r[:, 1]) + r[:, 2] * r[:, 2])
+    d = r / length[:, None]
+    nrm = P._dev(np.asarray(source_normals, dtype=np.float32).reshape(-1, 3), torch.float32)[si]
+    u1 = d / torch.linalg.vector_norm(d, dim=1, keepdim=True)
+    u2 = nrm / torch.linalg.vector_norm(nrm, dim=1, keepdim=True)
+    # angle(): arccos of the dot product clamped to [-1, 1] in FP64, stored as float32 (rayfunctions.py:436-448)
+    ang = torch.arccos((u1 * u2).sum(1).double().clamp(-1.0, 1.0)).float()
+    area = np.nan_to_num(np.asarray(vertex_area, dtype=np.float64).reshape(-1), nan=0.0)
+    if area.size == 1:
+        portion = torch.ones_like(ang, dtype=torch.float64) if area[0] == 0 else \
+            area[0] * torch.cos(ang).abs().double()
+    else:
+        portion = torch.as_tensor(area, device=dev)[si] * torch.cos(ang).abs().double()
+    portion = torch.where(ang.abs().double() > np.pi / 2, torch.zeros_like(portion), portion)
+    # patternsort (rayfunctions.py:462-468): the sum over each shell point's visible sources
+    total = torch.zeros(n_snk, dtype=torch.float64, device=dev).index_add_(0, mi, portion)
+    visible = total.float().cpu().numpy().reshape(len(elev_range), len(az_range))
+    shell.point_data["Projected_Area"] = visible.reshape(-1, 1)
+    return visible, shell

@@ -15,6 +15,7 @@ Reference behaviour restated here (paths within LyceanEM-Python):
   - one-bounce composition: lyceanem/models/frequency_domain.py:195-264
   - source sum to sink fields: lyceanem/models/frequency_domain.py:847-849
   - far-field E_theta/E_phi: lyceanem/models/frequency_domain.py:179-190
+  - visiblespace's projected-area sum per shell point: lyceanem/raycasting/rayfunctions.py:316-427
 """
 import ctypes
 import os
@@ -243,6 +244,28 @@ def numba_masks(src, snk, scat, tris12):
     m2 = mask_brute(scat, snk, tris12, **kw) if P else np.zeros((0, _f3(snk).shape[0]), bool)
     m3 = mask_brute(scat, scat, tris12, **kw) if P else np.zeros((0, 0), bool)
     return m0, m1, m2, m3
+
+
+def visible_patterns(src, src_normals, shell, mask, vertex_area):
+    """Per shell point, the summed projected area of the sources that see it: visiblespace's sum
+    (lyceanem/raycasting/rayfunctions.py:316-427) from the numba-rule mask [sources, shell points].
+    A visible pair adds area_n |cos angle| (angle between the float32 ray direction and the source
+    normal, in FP64 here), nothing past pi / 2; a single zero area counts each visible pair as 1 and
+    NaN areas count as 0.  Returns float64 [shell points]."""
+    src, shell = _f3(src).astype(np.float64), _f3(shell).astype(np.float64)
+    nrm = _f3(src_normals).astype(np.float64)
+    area = np.nan_to_num(np.asarray(vertex_area, np.float64).reshape(-1), nan=0.0)
+    n, m = np.nonzero(mask)
+    d = shell[m] - src[n]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    u = nrm[n] / np.linalg.norm(nrm[n], axis=1, keepdims=True)
+    c = np.clip(np.sum(d * u, axis=1), -1.0, 1.0)
+    if area.size == 1:
+        part = np.ones_like(c) if area[0] == 0 else area[0] * np.abs(c)
+    else:
+        part = area[n] * np.abs(c)
+    part[c < 0] = 0.0
+    return np.bincount(m, weights=part, minlength=shell.shape[0])
 
 
 def numba_path_index(N, M, P, m0, m1, m2, m3, max_scatter, line_of_sight=True):

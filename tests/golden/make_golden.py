@@ -24,7 +24,8 @@ Fixtures:
                           numba_sim.py for what it reproduces and what it cannot):
                           workchunkingv2's path index and ray count
                           (lyceanem/raycasting/rayfunctions.py:2681-2955) for one, two and three
-                          interactions, with and without line of sight; EMGPUFreqDomain
+                          interactions, with and without line of sight; visiblespace (:316-427) on
+                          an elevation-major shell standing in for pyvista's; EMGPUFreqDomain
                           (lyceanem/electromagnetics/empropagation.py:2197-2410) on those paths at
                           two wavelengths and with magnetic sources; TimeDomainv3 (:2910-3170) on a
                           one-block path list, with 400 and with 120 samples.  Written last: the
@@ -285,6 +286,29 @@ def numba_engine():
         out[f"index_{key}"], out[f"rays_{key}"] = idx, np.int64(rays)
         index[key] = idx
         print("  workchunkingv2", key, idx.shape, rays)
+    # visiblespace (rayfunctions.py:316-427) on scene a's sources with seeded normals and a 4 m shell; the
+    # shell comes from an elevation-major sphere standing in for targets.spherical_field (pyvista is absent)
+    def sphere(az_range, elev_range, outward_normals=False, field_radius=1.0):
+        E, A = np.meshgrid(np.deg2rad(elev_range), np.deg2rad(az_range), indexing="ij")
+        d = np.stack([np.cos(E) * np.cos(A), np.cos(E) * np.sin(A), np.sin(E)], -1).reshape(-1, 3)
+        return types.SimpleNamespace(points=(field_radius * d).astype(np.float32),
+                                     point_data={"Normals": (d if outward_normals else -d).astype(np.float32)})
+    RF.TG.spherical_field = sphere
+    sc = scenes["a"]
+    rng = np.random.default_rng(21)
+    vs_nrm = rng.normal(size=sc["src"].shape).astype(np.float32)
+    vs_nrm /= np.linalg.norm(vs_nrm, axis=1, keepdims=True)
+    vs_area = rng.uniform(0.5, 1.5, sc["src"].shape[0])
+    vs_area[2] = np.nan
+    out["vs_normals"], out["vs_area"] = vs_nrm, vs_area
+    for label, area, az, el in (("ones", np.array([0.0]), None, None), ("one_area", np.array([0.7]), None, None),
+                                ("areas", vs_area, np.linspace(-180.0, 180.0, 13), np.linspace(-90.0, 90.0, 7))):
+        kw = {} if az is None else dict(az_range=az, elev_range=el)
+        pat, shell = RF.visiblespace(types.SimpleNamespace(points=sc["src"]), vs_nrm, environment(sc),
+                                     vertex_area=np.array(area, copy=True), shell_range=4.0, **kw)
+        out[f"vs_{label}"] = np.asarray(pat)
+        out[f"vs_{label}_shell"] = np.asarray(shell.points)
+        print("  visiblespace", label, np.asarray(pat).shape, float(np.nansum(pat)))
     # per-path products: (case, wavelength, magnetic sources)
     alpha = 0.02
     for key, lam, mag in (("a2los", 0.5, 0), ("a2los", 0.05, 0), ("a2los", 0.5, 3), ("b3los", 0.5, 0)):

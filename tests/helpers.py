@@ -64,3 +64,13 @@ def numba_golden_magnetic(n_points, magnetic):
     imp = np.full(n_points, np.sqrt(np.float32(1.25663706212e-6).astype(np.float64)
                                     / np.float32(8.8541878176e-12).astype(np.float64)), np.float32)
     return mag, imp
+
+
+# visiblespace fixture cases: (label, vertex_area key or value, az_range, elev_range); shell radius 4 m
+NUMBA_VS_SHELL = 4.0
+
+
+def numba_vs_cases(d):
+    return [("ones", np.array([0.0]), None, None), ("one_area", np.array([0.7]), None, None),
+            ("areas", d["vs_area"], np.linspace(-180.0, 180.0, 13), np.linspace(-90.0, 90.0, 7))]
+

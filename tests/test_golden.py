@@ -83,8 +83,8 @@ def test_numba_engine_golden_oracle():
     executing workchunkingv2, EMGPUFreqDomain and TimeDomainv3 from the reference's source,
     tests/golden/numba_sim.py): path index and ray count row for row, per-path products and the time map
     within the reference's own float32 rounding."""
-    from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, numba_golden, numba_golden_magnetic,
-                         numba_golden_scene, numba_index_key, rel_err)
+    from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, NUMBA_VS_SHELL, numba_golden,
+                         numba_golden_magnetic, numba_golden_scene, numba_index_key, numba_vs_cases, rel_err)
     d = numba_golden()
     for scene, ms, los in NUMBA_INDEX_CASES:
         src, snk, scat, v, f, _, _, _ = numba_golden_scene(d, scene)
@@ -93,6 +93,15 @@ def test_numba_engine_golden_oracle():
         key = numba_index_key(scene, ms, los)
         assert np.array_equal(idx, d[f"index_{key}"]), key
         assert rays == int(d[f"rays_{key}"]), key
+    src, _, _, v, f, _, _, _ = numba_golden_scene(d, "a")
+    for label, area, az, el in numba_vs_cases(d):
+        shell = d[f"vs_{label}_shell"]
+        mask = O.numba_masks(src, shell, np.zeros((0, 3), np.float32), O.pack_triangles(v, f))[0]
+        pat = O.visible_patterns(src, d["vs_normals"], shell, mask, area)
+        ref = d[f"vs_{label}"].reshape(-1)
+        if label == "ones":
+            assert np.array_equal(pat, ref)  # visible pairs in front of their source, counted
+        assert rel_err(pat, ref) < 1e-5, label
     for key, lam, mag, tol in NUMBA_FIELD_CASES:
         src, snk, _, _, _, pos, nrm, w = numba_golden_scene(d, key[0])
         m, imp = numba_golden_magnetic(pos.shape[0], mag)

@@ -9,8 +9,8 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, numba_golden, numba_golden_scene,
-                     numba_index_key, random_scene, rel_err)
+from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, NUMBA_VS_SHELL, numba_golden,
+                     numba_golden_scene, numba_index_key, numba_vs_cases, random_scene, rel_err)
 
 pytestmark = pytest.mark.gpu
 
@@ -189,5 +189,28 @@ def test_emgpufreqdomain_reference_golden(key, lam, magnetic, tol):
     pts["permeability"] = 1.25663706212e-6
     S = EMGPUFreqDomain(src.shape[0], snk.shape[0], d[f"index_{key}"], pts, lam, NUMBA_ALPHA, 2 * np.pi / lam)
     assert rel_err(S, d[f"field_{key}_{lam}_{magnetic}"]) < tol
+    _no_device_errors()
+
+
+def test_visiblespace_reference_golden():
+    """visiblespace against the reference's own function (fixture executed from its source on the same
+    elevation-major shell): visible pairs counted exactly, projected areas within 1e-5."""
+    from lyceanem_gb300 import raycasting as RC
+    from lyceanem_gb300.geometry import Mesh
+    d = numba_golden()
+    src, _, _, v, f, _, _, _ = numba_golden_scene(d, "a")
+    for label, area, az, el in numba_vs_cases(d):
+        kw = {} if az is None else dict(az_range=az, elev_range=el)
+        area_in = np.array(area, copy=True)
+        pat, shell = RC.visiblespace(Mesh(src), d["vs_normals"], (v, f), vertex_area=area_in,
+                                     shell_range=NUMBA_VS_SHELL, **kw)
+        ref = d[f"vs_{label}"]
+        assert np.array_equal(np.asarray(shell.points), d[f"vs_{label}_shell"])
+        assert pat.shape == ref.shape and pat.dtype == np.float32
+        if label == "ones":
+            assert np.array_equal(pat, ref)
+        assert rel_err(pat, ref) < 1e-5, label
+        assert np.array_equal(shell.point_data["Projected_Area"].reshape(-1), pat.reshape(-1))
+        assert np.array_equal(np.isnan(area_in), np.isnan(np.asarray(area)))  # the caller's areas stay as given
     _no_device_errors()
 
