@@ -219,6 +219,8 @@ def vector_mapping(local_E_vector, point_normal, rotation_matrix):
     v = (n x u)/|u x n|; result = local @ [u; v; n]."""
     dtype = np.asarray(local_E_vector).dtype
     n = np.matmul(np.asarray(point_normal).astype(dtype), rotation_matrix)
+    if not np.iscomplexobj(np.zeros(0, dtype)):
+        n = np.real(n)  # the axes of a real E-vector are real (the reference's store drops the zero imaginary part)
     axes = np.eye(3)
     uvn = np.zeros((3, 3), dtype=dtype)
     uvn[2, :] = n

@@ -28,7 +28,9 @@ Fixtures:
                           an elevation-major shell standing in for pyvista's; EMGPUFreqDomain
                           (lyceanem/electromagnetics/empropagation.py:2197-2410) on those paths at
                           two wavelengths and with magnetic sources; TimeDomainv3 (:2910-3170) on a
-                          one-block path list, with 400 and with 120 samples.  Written last: the
+                          one-block path list, with 400 and with 120 samples; and the model-level
+                          calculate_scattering(cuda=False) (lyceanem/models/frequency_domain.py:
+                          267-718) for direct, one- and two-bounce paths.  Written last: the
                           stand-in modules stay installed.
 Usage: python tests/golden/make_golden.py [reference_root] [--only NAME]
 """
@@ -309,6 +311,34 @@ def numba_engine():
         out[f"vs_{label}"] = np.asarray(pat)
         out[f"vs_{label}_shell"] = np.asarray(shell.points)
         print("  visiblespace", label, np.asarray(pat).shape, float(np.nansum(pat)))
+    # the model-level numba branch: calculate_scattering(cuda=False) (lyceanem/models/frequency_domain.py:267-718)
+    # on meshio-like meshes; its module imports acceleration_structures, whose compiled `em` it never calls here
+    em = types.ModuleType("lyceanem.em")
+    for name in ("bin_counts_to_numpy", "bin_triangles_to_numpy", "calculate_scattering_brute_force",
+                 "calculate_scattering_tiles"):
+        setattr(em, name, None)
+    sys.modules["lyceanem.em"] = em
+    import meshio
+    import lyceanem.models.frequency_domain as FD
+    for name, sc in (("m", _numba_scene(8, 5, 50, 90, 20)), ("d", _numba_scene(9, 3, 20, 40, 8))):
+        for k, val in sc.items():
+            out[f"{name}_{k}"] = val
+        n_src = sc["src"].shape[0]
+        solid = meshio.Mesh(sc["verts"], [("triangle", sc["faces"])])
+        sk = meshio.Mesh(sc["snk"], [], point_data={"Normals": sc["snk_n"]})
+        sp = meshio.Mesh(sc["scat"], [], point_data={"Normals": sc["scat_n"]})
+        cases = [(2, True, False, False)] if name == "d" else \
+            [(0, True, False, False), (0, True, False, True), (1, True, False, False), (1, False, False, False),
+             (1, True, True, False)]
+        for scattering, los, elements, project in cases:
+            ap = meshio.Mesh(sc["src"], [], point_data={"Normals": np.tile([[0, 0, 1.0]], (n_src, 1)),
+                                                       "Area": np.full(n_src, 0.5)})
+            res = FD.calculate_scattering(ap, sk, solid, np.array([[1.0, 0.0, 0.0]]), scatter_points=sp,
+                                          wavelength=0.5, scattering=scattering, elements=elements, los=los,
+                                          project_vectors=project, beta=2 * np.pi / 0.5, cuda=False)
+            key = f"model_{name}_{scattering}{int(los)}{int(elements)}{int(project)}"
+            out[key] = np.stack(res, -1)
+            print("  calculate_scattering(cuda=False)", key, out[key].shape)
     # per-path products: (case, wavelength, magnetic sources)
     alpha = 0.02
     for key, lam, mag in (("a2los", 0.5, 0), ("a2los", 0.05, 0), ("a2los", 0.5, 3), ("b3los", 0.5, 0)):

@@ -251,6 +251,50 @@ def _atomic_min(arr, idx, val):
     return old
 
 
+def _make_meshio():
+    """meshio's Mesh and CellBlock as plain containers (the reference's model code takes meshes by
+    isinstance and reads .points, .cells[i].type / .data and .point_data)."""
+    m = types.ModuleType("meshio")
+
+    class CellBlock:
+        def __init__(self, cell_type, data):
+            self.type = cell_type
+            self.data = np.asarray(data)
+
+    class Mesh:
+        def __init__(self, points, cells, point_data=None, cell_data=None):
+            self.points = np.asarray(points)
+            self.cells = [c if isinstance(c, CellBlock) else CellBlock(c[0], c[1]) for c in cells]
+            self.point_data = dict(point_data or {})
+            self.cell_data = dict(cell_data or {})
+
+    m.Mesh, m.CellBlock = Mesh, CellBlock
+    return m
+
+
+class _StubFinder:
+    """Import hook giving an empty package for every module under `roots` (plotting and meshing
+    libraries the reference imports at module level but the numba path never calls)."""
+
+    def __init__(self, roots):
+        self.roots = roots
+
+    def find_spec(self, name, path=None, target=None):
+        import importlib.machinery
+        if name.split(".")[0] not in self.roots:
+            return None
+        return importlib.machinery.ModuleSpec(name, self, is_package=True)
+
+    def create_module(self, spec):
+        m = types.ModuleType(spec.name)
+        m.__path__ = []
+        m.__getattr__ = _stub_attr
+        return m
+
+    def exec_module(self, module):
+        pass
+
+
 def _stub_attr(attr):
     if attr.startswith("__"):
         raise AttributeError(attr)
@@ -277,12 +321,9 @@ def install():
     cp.asnumpy = lambda a: np.array(a).view(np.ndarray)
     cp.asarray = _device
     sys.modules["cupy"] = cp
-    for name in ("meshio", "gmsh", "pyvista", "matplotlib", "matplotlib.cm", "importlib_resources"):
-        if name not in sys.modules:
-            m = types.ModuleType(name)
-            m.__getattr__ = _stub_attr
-            sys.modules[name] = m
-    sys.modules["matplotlib"].cm = sys.modules["matplotlib.cm"]
+    sys.modules["meshio"] = _make_meshio()
+    sys.meta_path.insert(0, _StubFinder(("gmsh", "pyvista", "matplotlib", "mpl_toolkits", "pylab",
+                                         "importlib_resources", "vtk")))
 
 
 def freeze_float_globals(module):

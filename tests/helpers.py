@@ -74,3 +74,13 @@ def numba_vs_cases(d):
     return [("ones", np.array([0.0]), None, None), ("one_area", np.array([0.7]), None, None),
             ("areas", d["vs_area"], np.linspace(-180.0, 180.0, 13), np.linspace(-90.0, 90.0, 7))]
 
+
+# calculate_scattering(cuda=False) fixture cases: (scene, scattering, los, elements, project_vectors); aperture
+# normals +z and areas 0.5, desired E axis +x, lambda = 0.5 m, beta = 2 pi / lambda
+NUMBA_MODEL_CASES = [("m", 0, True, False, False), ("m", 0, True, False, True), ("m", 1, True, False, False),
+                     ("m", 1, False, False, False), ("m", 1, True, True, False), ("d", 2, True, False, False)]
+
+
+def numba_model_key(scene, scattering, los, elements, project):
+    return f"model_{scene}_{scattering}{int(los)}{int(elements)}{int(project)}"
+

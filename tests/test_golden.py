@@ -161,3 +161,26 @@ def test_numba_stand_in_typing():
     buf, out = np.zeros(8, np.int64), np.zeros(8, np.int64)
     kern[2, 4](buf, out)
     assert kern.lockstep and out.tolist() == [1, 2, 3, 0, 5, 6, 7, 4]
+
+
+def test_numba_model_golden_oracle():
+    """The oracle's composition of the numba branch of calculate_scattering (visibility rule, path index,
+    per-path product, source sum) against the reference's own calculate_scattering(cuda=False) run under the
+    numba stand-in, for the cases without vector projection."""
+    from helpers import NUMBA_MODEL_CASES, numba_golden, numba_golden_scene, numba_model_key, rel_err
+    d = numba_golden()
+    beta = 2 * np.pi / 0.5
+    for scene, scattering, los, elements, project in NUMBA_MODEL_CASES:
+        if project:
+            continue
+        src, snk, scat, v, f, pos, nrm, _ = numba_golden_scene(d, scene)
+        N, M, Pn = src.shape[0], snk.shape[0], scat.shape[0]
+        Esrc = np.tile([[0.5 if scattering == 0 else 1.0, 0.0, 0.0]], (N, 1)).astype(np.complex64)
+        masks = O.numba_masks(src, snk, scat, O.pack_triangles(v, f))
+        idx, _ = O.numba_path_index(N, M, Pn, *masks, scattering + 1, line_of_sight=los)
+        w = np.ones((N + M + Pn, 3), np.complex128)
+        w[:N] = Esrc
+        net = O.path_field(idx, pos, nrm, w, N, M, 0.0, beta)
+        ref = d[numba_model_key(scene, scattering, los, elements, project)]
+        assert rel_err(net if elements else net.sum(0), ref) < 1e-5, (scene, scattering, los, elements)
+

@@ -9,8 +9,9 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, NUMBA_VS_SHELL, numba_golden,
-                     numba_golden_scene, numba_index_key, numba_vs_cases, random_scene, rel_err)
+from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, NUMBA_MODEL_CASES, NUMBA_VS_SHELL,
+                     numba_golden, numba_golden_scene, numba_index_key, numba_model_key, numba_vs_cases,
+                     random_scene, rel_err)
 
 pytestmark = pytest.mark.gpu
 
@@ -212,5 +213,24 @@ def test_visiblespace_reference_golden():
         assert rel_err(pat, ref) < 1e-5, label
         assert np.array_equal(shell.point_data["Projected_Area"].reshape(-1), pat.reshape(-1))
         assert np.array_equal(np.isnan(area_in), np.isnan(np.asarray(area)))  # the caller's areas stay as given
+    _no_device_errors()
+
+
+@pytest.mark.parametrize("scene,scattering,los,elements,project", NUMBA_MODEL_CASES)
+def test_calculate_scattering_numba_branch_reference_golden(scene, scattering, los, elements, project):
+    """calculate_scattering(cuda=False) against the reference's own model function (fixture executed from its
+    source under the numba stand-in) within 1e-5."""
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import frequency_domain as FD
+    d = numba_golden()
+    src, snk, scat, v, f, _, _, _ = numba_golden_scene(d, scene)
+    N = src.shape[0]
+    ap = Mesh(src, point_data={"Normals": np.tile([[0, 0, 1.0]], (N, 1)), "Area": np.full(N, 0.5)})
+    sk = Mesh(snk, point_data={"Normals": d[f"{scene}_snk_n"]})
+    sc = Mesh(scat, point_data={"Normals": d[f"{scene}_scat_n"]})
+    out = FD.calculate_scattering(ap, sk, Mesh(v, [("triangle", f)]), np.array([[1.0, 0.0, 0.0]]), scatter_points=sc,
+                                  wavelength=0.5, scattering=scattering, elements=elements, los=los,
+                                  project_vectors=project, beta=2 * np.pi / 0.5, cuda=False)
+    assert rel_err(np.stack(out, -1), d[numba_model_key(scene, scattering, los, elements, project)]) < 1e-5
     _no_device_errors()
 
