@@ -55,18 +55,21 @@ def spherical_field(az_range, elev_range, outward_normals=False, field_radius=1.
     first elevation, then the next), with normals and theta/phi.
 
     Mirrors lyceanem/geometry/targets.py:448-497: inward normals unless
-    outward_normals; point_data holds "Normals", "theta_(Radians)" (polar angle
-    from +z) and "phi_(Radians)" (azimuth).  Point order is this package's own."""
+    outward_normals; point_data holds "Normals", "Radial_Distance_(m)",
+    "theta_(Radians)" and "phi_(Radians)", formed from the stored points as
+    theta_phi_r does (lyceanem/geometry/geometryfunctions.py:447-470: arccos of
+    z / r and arctan2(y, x)).  Point order is this package's own."""
     az = np.deg2rad(np.asarray(az_range, dtype=np.float64))
     el = np.deg2rad(np.asarray(elev_range, dtype=np.float64))
     E, A = np.meshgrid(el, az, indexing="ij")
     E, A = E.ravel(), A.ravel()
     d = np.stack([np.cos(E) * np.cos(A), np.cos(E) * np.sin(A), np.sin(E)], axis=1)
-    pts = field_radius * d
+    pts = (field_radius * d).astype(np.float32)
     nrm = d if outward_normals else -d
-    theta = np.pi / 2 - E
-    return Mesh(points=pts.astype(np.float32), point_data={
-        "Normals": nrm.astype(np.float32), "theta_(Radians)": theta, "phi_(Radians)": A})
+    r = np.linalg.norm(pts - np.zeros((1, 3)), axis=1)
+    return Mesh(points=pts, point_data={
+        "Normals": nrm.astype(np.float32), "Radial_Distance_(m)": r, "theta_(Radians)": np.arccos(pts[:, 2] / r),
+        "phi_(Radians)": np.arctan2(pts[:, 1], pts[:, 0])})
 
 
 _PLY_TYPES = {"char": "i1", "int8": "i1", "uchar": "u1", "uint8": "u1", "short": "i2", "int16": "i2",

@@ -60,6 +60,12 @@ def tile_geometry(points, n_cells):
     return g
 
 
+def em_float(x):
+    """A scalar as the reference's compiled em module receives it: its bindings take alpha and beta as
+    C++ float (lyceanem/src/frequency_domain_models.cu:44-47, 190-195), so they arrive rounded to float32."""
+    return float(np.float32(x))
+
+
 class _DeviceScene:
     """Packed triangles on the device plus an optional uniform grid."""
 
@@ -117,6 +123,7 @@ class Tile_acceleration_structure:
 
     def calculate_scattering(self, source_mesh, sink_mesh, alpha, beta, wavelength, self_to_self, chunk_count=1):
         del wavelength  # unused by the field formula, as in the reference
+        alpha, beta = em_float(alpha), em_float(beta)
         return self.device.network(source_mesh, sink_mesh, alpha, beta, self_to_self, chunk_count)
 
     def sink_field(self, source_mesh, sink_mesh, alpha, beta, wavelength=None, self_to_self=False):
@@ -169,6 +176,7 @@ class Brute_Force_acceleration_structure:
 
     def calculate_scattering(self, source_mesh, sink_mesh, alpha, beta, wavelength, self_to_self, chunk_count=1):
         del wavelength
+        alpha, beta = em_float(alpha), em_float(beta)
         return self.device.network(source_mesh, sink_mesh, alpha, beta, self_to_self, chunk_count)
 
     def sink_field(self, source_mesh, sink_mesh, alpha, beta, wavelength=None, self_to_self=False):

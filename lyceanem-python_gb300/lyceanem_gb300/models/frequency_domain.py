@@ -261,7 +261,7 @@ def _numba_branch(aperture_coords, sink_coords, antenna_solid, desired_E_axis, s
 
 def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_axis, scatter_points=None,
                          wavelength=1.0, scattering=0, elements=False, los=True, project_vectors=False,
-                         antenna_axes=np.eye(3), multiE=False, alpha=0.0, beta=(np.pi * 2) / 1.0, cuda=True,
+                         antenna_axes=np.eye(3), multiE=False, alpha=0.0, beta=(np.pi * 2) / 1.0, cuda=False,
                          acceleration_structure=None, chunks=1, permittivity=8.8541878176e-12,
                          permeability=1.25663706212e-6, grid_cell=None):
     """Ex, Ey, Ez at the sinks (elements=False: complex64 [M] each, summed over
@@ -280,6 +280,7 @@ def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_
                              grid_cell)
     del los
     cull, eps = True, P.EPSILON
+    alpha, beta = acceleration_structures.em_float(alpha), acceleration_structures.em_float(beta)
     acc = _as_structure(antenna_solid, acceleration_structure, grid_cell)
     src = np.asarray(aperture_coords.points, dtype=np.float32)
     snk = np.asarray(sink_coords.points, dtype=np.float32)
@@ -334,14 +335,16 @@ def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_
 
 def calculate_farfield(aperture_coords, antenna_solid, desired_E_axis, az_range=None, el_range=None,
                        scatter_points=None, wavelength=1.0, farfield_distance=2.0, scattering=0, elements=False,
-                       los=True, project_vectors=False, cuda=True, antenna_axes=np.eye(3), alpha=0.0,
+                       los=True, project_vectors=False, cuda=False, antenna_axes=np.eye(3), alpha=0.0,
                        beta=(np.pi * 2) / 1.0, grid_cell=None):
-    """E_theta, E_phi on a far-field sphere (lyceanem/models/frequency_domain.py:94-192)."""
+    """E_theta, E_phi on a far-field sphere (lyceanem/models/frequency_domain.py:94-192).  As in the
+    reference, farfield_distance reaches spherical_field as its third positional argument, outward_normals
+    (:159): the sinks lie on the unit sphere, with outward normals unless farfield_distance is 0."""
     if az_range is None:
         az_range = np.linspace(-180.0, 180.0, 19)
     if el_range is None:
         el_range = np.linspace(-90.0, 90.0, 19)
-    sink_coords = spherical_field(az_range, el_range, field_radius=farfield_distance)
+    sink_coords = spherical_field(az_range, el_range, farfield_distance)
     Ex, Ey, Ez = calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_axis,
                                       scatter_points=scatter_points, wavelength=wavelength, scattering=scattering,
                                       elements=elements, los=los, project_vectors=project_vectors,

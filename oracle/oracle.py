@@ -222,8 +222,9 @@ def farfield_theta_phi(E, theta, phi):
 
 # ---------------------------------------------------------------- numba engine
 # Restatement of the numba engine's path list and per-path product (test
-# infrastructure).  The engine itself cannot run here (numba and cupy are not
-# installed), so these follow its source:
+# infrastructure), following its source and checked against the engine's own
+# outputs on small scenes (tests/golden/numba_engine.npz, made by running the
+# engine under a stand-in for numba and cupy):
 #   path index   workchunkingv2 / create_model_index / rayHits1Dv2
 #                (lyceanem/raycasting/rayfunctions.py:2624-2955, 1845-1878)
 #   path product freqdomainkernal / sourcelaunchtransformGPU / lossy_propagation

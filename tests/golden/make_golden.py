@@ -30,8 +30,14 @@ Fixtures:
                           two wavelengths and with magnetic sources; TimeDomainv3 (:2910-3170) on a
                           one-block path list, with 400 and with 120 samples; and the model-level
                           calculate_scattering(cuda=False) (lyceanem/models/frequency_domain.py:
-                          267-718) for direct, one- and two-bounce paths.  Written last: the
-                          stand-in modules stay installed.
+                          267-718) for direct, one- and two-bounce paths.
+  cuda_model.npz          the reference's CUDA-engine model layer (calculate_scattering(cuda=True),
+                          calculate_scattering_cuda, Tile_acceleration_structure.calculate_scattering,
+                          calculate_farfield; lyceanem/models/frequency_domain.py:94-264, 719-926,
+                          lyceanem/models/acceleration_structures.py:72-115) executed from its source
+                          with its compiled `em` module replaced by the oracle's per-pair network.
+The numba_engine and cuda_model fixtures install stand-in modules, so each runs in its own process
+(--only NAME); the others run together.
 Usage: python tests/golden/make_golden.py [reference_root] [--only NAME]
 """
 import ast
@@ -367,9 +373,92 @@ def numba_engine():
     np.savez_compressed(os.path.join(HERE, "numba_engine.npz"), **out)
 
 
+def cuda_model():
+    """The reference's CUDA-engine model layer (calculate_scattering(cuda=True), calculate_scattering_cuda,
+    Tile_acceleration_structure.calculate_scattering, calculate_farfield) run from its source, with its
+    compiled `em` module replaced by the oracle: the per-pair networks are the oracle's (pinned to the
+    reference's device code by reference_pairs.npz), everything composed around them is the reference's."""
+    sys.path.insert(0, HERE)
+    import numba_sim
+    numba_sim.install()
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import oracle as O
+    em = types.ModuleType("lyceanem.em")
+
+    def bin_counts_to_numpy(vertices, tri_index, ny, nz, ymin, cell, zmin):
+        counts = np.zeros(int(ny) * int(nz), np.int32)
+        counts[0] = np.asarray(tri_index).shape[0]  # one bin: the oracle's networks do not use the bins
+        return counts
+
+    def bin_triangles_to_numpy(vertices, tri_index, ny, nz, ymin, cell, zmin, counts, total):
+        return np.ascontiguousarray(np.asarray(tri_index, np.int32).ravel())
+
+    def calculate_scattering_tiles(source, end, vertices, wavelength, exr, exi, eyr, eyi, ezr, ezi, normal, xmin,
+                                   xmax, ymin, ymax, zmin, zmax, tile, counts, binned, ny, nz, n_binned, alpha,
+                                   beta, self_to_self):
+        src, snk = np.asarray(source, np.float32), np.asarray(end, np.float32)
+        tris = O.pack_triangles(np.asarray(vertices, np.float32), np.asarray(binned, np.int32).reshape(-1, 3))
+        E = np.stack([np.asarray(exr) + 1j * np.asarray(exi), np.asarray(eyr) + 1j * np.asarray(eyi),
+                      np.asarray(ezr) + 1j * np.asarray(ezi)], 1)
+        S, _ = O.scattering_network(src, E, snk, np.asarray(normal, np.float32)[src.shape[0]:], tris,
+                                    float(np.float32(alpha)), float(np.float32(beta)), self_to_self=bool(self_to_self))
+        return S.astype(np.complex64).view(np.float32).ravel()
+
+    em.bin_counts_to_numpy, em.bin_triangles_to_numpy = bin_counts_to_numpy, bin_triangles_to_numpy
+    em.calculate_scattering_tiles = calculate_scattering_tiles
+    em.calculate_scattering_brute_force = None
+    sys.modules["lyceanem.em"] = em
+    sys.path.insert(0, REF)
+    import meshio
+    import lyceanem.geometry.geometryfunctions as GF
+    import lyceanem.geometry.targets as TL
+    import lyceanem.models.frequency_domain as FD
+
+    def sphere(az_range, elev_range, outward_normals=False, field_radius=1.0):
+        # elevation-major sphere standing in for pyvista's; theta / phi from the reference's theta_phi_r
+        E, A = np.meshgrid(np.deg2rad(elev_range), np.deg2rad(az_range), indexing="ij")
+        d = np.stack([np.cos(E) * np.cos(A), np.cos(E) * np.sin(A), np.sin(E)], -1).reshape(-1, 3)
+        m = meshio.Mesh((field_radius * d).astype(np.float32), [],
+                        point_data={"Normals": (d if outward_normals else -d).astype(np.float32)})
+        return GF.theta_phi_r(m)
+    TL.spherical_field = sphere
+
+    sc = _numba_scene(17, 5, 50, 90, 20)
+    out = {f"s_{k}": v for k, v in sc.items()}
+    n_src = sc["src"].shape[0]
+    lam = 0.04
+
+    def meshes():
+        ap = meshio.Mesh(sc["src"], [], point_data={"Normals": np.tile([[0, 0, 1.0]], (n_src, 1)),
+                                                   "Area": np.full(n_src, 0.5)})
+        sk = meshio.Mesh(sc["snk"], [], point_data={"Normals": sc["snk_n"]})
+        sp = meshio.Mesh(sc["scat"], [], point_data={"Normals": sc["scat_n"]})
+        return ap, sk, sp, meshio.Mesh(sc["verts"], [("triangle", sc["faces"])])
+
+    axis = np.array([[1.0, 0.0, 0.0]])
+    for label, kw in (("s0", {}), ("s0_elements", dict(elements=True)), ("s0_project", dict(project_vectors=True)),
+                      ("s1", dict(scattering=1)), ("s1_elements", dict(scattering=1, elements=True)),
+                      ("s1_chunks2", dict(scattering=1, elements=True, chunks=2))):
+        ap, sk, sp, solid = meshes()
+        res = FD.calculate_scattering(ap, sk, solid, axis, scatter_points=sp, wavelength=lam, beta=2 * np.pi / lam,
+                                      cuda=True, **kw)
+        out[f"cs_{label}"] = np.stack(res, -1)
+        print("  calculate_scattering(cuda=True)", label, out[f"cs_{label}"].shape)
+    for label, kw in (("ff0", {}), ("ff1", dict(scattering=1))):
+        ap, _, sp, solid = meshes()
+        et, ep = FD.calculate_farfield(ap, solid, axis, az_range=np.linspace(-180, 180, 9),
+                                       el_range=np.linspace(-90, 90, 5), scatter_points=sp, wavelength=lam,
+                                       farfield_distance=5.0, beta=2 * np.pi / lam, cuda=True, **kw)
+        out[f"{label}_theta"], out[f"{label}_phi"] = np.asarray(et), np.asarray(ep)
+        print("  calculate_farfield(cuda=True)", label, np.asarray(et).shape)
+    np.savez_compressed(os.path.join(HERE, "cuda_model.npz"), **out)
+
+
 if __name__ == "__main__":
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
-    for fn in (convert_triangles, vector_mapping_cases, tile_structure, excitation_cases, numba_engine):
-        if only is None or fn.__name__ == only:
+    plain = (convert_triangles, vector_mapping_cases, tile_structure, excitation_cases)
+    with_stand_ins = (numba_engine, cuda_model)  # each installs stand-in modules: one per process
+    for fn in plain + with_stand_ins:
+        if (only is None and fn in plain) or (only is not None and fn.__name__ == only):
             fn()
     print("golden fixtures written to", HERE)

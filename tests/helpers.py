@@ -84,3 +84,18 @@ NUMBA_MODEL_CASES = [("m", 0, True, False, False), ("m", 0, True, False, True), 
 def numba_model_key(scene, scattering, los, elements, project):
     return f"model_{scene}_{scattering}{int(los)}{int(elements)}{int(project)}"
 
+
+# CUDA-engine model fixtures (tests/golden/cuda_model.npz): calculate_scattering(cuda=True) cases as keyword
+# arguments, on scene "s" (5 sources, 50 sinks, 20 scatter points, 90 triangles), areas 0.5, E axis +x,
+# lambda = 0.04 m; far fields on 9 azimuths x 5 elevations with farfield_distance 5.
+CUDA_MODEL_LAMBDA = 0.04
+CUDA_MODEL_CASES = [("s0", {}), ("s0_elements", dict(elements=True)), ("s0_project", dict(project_vectors=True)),
+                    ("s1", dict(scattering=1)), ("s1_elements", dict(scattering=1, elements=True)),
+                    ("s1_chunks2", dict(scattering=1, elements=True, chunks=2))]
+CUDA_FARFIELD_CASES = [("ff0", {}), ("ff1", dict(scattering=1))]
+
+
+def cuda_model_golden():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cuda_model.npz"))
+

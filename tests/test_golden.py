@@ -184,3 +184,29 @@ def test_numba_model_golden_oracle():
         ref = d[numba_model_key(scene, scattering, los, elements, project)]
         assert rel_err(net if elements else net.sum(0), ref) < 1e-5, (scene, scattering, los, elements)
 
+
+def test_cuda_model_golden_oracle():
+    """The oracle's composition of the CUDA engine's model layer (source sum, one bounce with the scatter
+    points excited by the summed source->scatter field, per-element networks, far-field projection) against
+    the reference's own model functions run on the oracle's per-pair networks."""
+    from helpers import CUDA_MODEL_LAMBDA, cuda_model_golden, rel_err
+    from lyceanem_gb300.geometry import spherical_field
+    d = cuda_model_golden()
+    g = lambda k: d[f"s_{k}"]  # noqa: E731
+    src, snk, snk_n, scat, scat_n = g("src"), g("snk"), g("snk_n"), g("scat"), g("scat_n")
+    tris = O.pack_triangles(g("verts"), g("faces"))
+    beta = float(np.float32(2 * np.pi / CUDA_MODEL_LAMBDA))  # the compiled em module takes beta as float32
+    E = np.tile([[0.5, 0.0, 0.0]], (src.shape[0], 1))
+    S0, _ = O.scattering_network(src, E, snk, snk_n, tris, 0.0, beta)
+    assert rel_err(S0.sum(0), d["cs_s0"]) < 1e-6
+    assert rel_err(S0, d["cs_s0_elements"]) < 1e-6
+    field, _ = O.onebounce_sink_field(src, E, snk, snk_n, scat, scat_n, 0.0, beta, tris12=tris)
+    assert rel_err(field, d["cs_s1"]) < 1e-6
+    sh = spherical_field(np.linspace(-180, 180, 9), np.linspace(-90, 90, 5), 5.0)  # unit sphere, outward
+    for label, bounce in (("ff0", False), ("ff1", True)):
+        pn = np.asarray(sh.point_data["Normals"])
+        F = (O.onebounce_sink_field(src, E, sh.points, pn, scat, scat_n, 0.0, beta, tris12=tris)[0] if bounce
+             else O.scattering_network(src, E, sh.points, pn, tris, 0.0, beta)[0].sum(0))
+        et, ep = O.farfield_theta_phi(F, sh.point_data["theta_(Radians)"], sh.point_data["phi_(Radians)"])
+        assert rel_err(et, d[f"{label}_theta"]) < 1e-6 and rel_err(ep, d[f"{label}_phi"]) < 1e-6, label
+

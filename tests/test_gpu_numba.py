@@ -9,7 +9,8 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import (NUMBA_ALPHA, NUMBA_FIELD_CASES, NUMBA_INDEX_CASES, NUMBA_MODEL_CASES, NUMBA_VS_SHELL,
+from helpers import (CUDA_FARFIELD_CASES, CUDA_MODEL_CASES, CUDA_MODEL_LAMBDA, NUMBA_ALPHA, NUMBA_FIELD_CASES,
+                     NUMBA_INDEX_CASES, NUMBA_MODEL_CASES, NUMBA_VS_SHELL, cuda_model_golden,
                      numba_golden, numba_golden_scene, numba_index_key, numba_model_key, numba_vs_cases,
                      random_scene, rel_err)
 
@@ -232,5 +233,42 @@ def test_calculate_scattering_numba_branch_reference_golden(scene, scattering, l
                                   wavelength=0.5, scattering=scattering, elements=elements, los=los,
                                   project_vectors=project, beta=2 * np.pi / 0.5, cuda=False)
     assert rel_err(np.stack(out, -1), d[numba_model_key(scene, scattering, los, elements, project)]) < 1e-5
+    _no_device_errors()
+
+
+def _cuda_model_meshes(d):
+    from lyceanem_gb300.geometry import Mesh
+    g = lambda k: d[f"s_{k}"]  # noqa: E731
+    n = g("src").shape[0]
+    ap = Mesh(g("src"), point_data={"Normals": np.tile([[0, 0, 1.0]], (n, 1)), "Area": np.full(n, 0.5)})
+    return (ap, Mesh(g("snk"), point_data={"Normals": g("snk_n")}),
+            Mesh(g("scat"), point_data={"Normals": g("scat_n")}), Mesh(g("verts"), [("triangle", g("faces"))]))
+
+
+@pytest.mark.parametrize("label,kw", CUDA_MODEL_CASES)
+def test_calculate_scattering_cuda_reference_golden(label, kw):
+    """calculate_scattering(cuda=True) against the reference's own model layer (calculate_scattering_cuda and
+    Tile_acceleration_structure.calculate_scattering executed from its source on the oracle's per-pair
+    networks) within 1e-5."""
+    from lyceanem_gb300.models import frequency_domain as FD
+    d = cuda_model_golden()
+    ap, sk, sc, solid = _cuda_model_meshes(d)
+    out = FD.calculate_scattering(ap, sk, solid, np.array([[1.0, 0.0, 0.0]]), scatter_points=sc,
+                                  wavelength=CUDA_MODEL_LAMBDA, beta=2 * np.pi / CUDA_MODEL_LAMBDA, cuda=True, **kw)
+    assert rel_err(np.stack(out, -1), d[f"cs_{label}"]) < 1e-5
+    _no_device_errors()
+
+
+@pytest.mark.parametrize("label,kw", CUDA_FARFIELD_CASES)
+def test_calculate_farfield_reference_golden(label, kw):
+    """calculate_farfield(cuda=True) against the reference's own function (the same unit-sphere sinks with
+    outward normals that its positional farfield_distance produces) within 1e-5."""
+    from lyceanem_gb300.models import frequency_domain as FD
+    d = cuda_model_golden()
+    ap, _, sc, solid = _cuda_model_meshes(d)
+    et, ep = FD.calculate_farfield(ap, solid, np.array([[1.0, 0.0, 0.0]]), az_range=np.linspace(-180, 180, 9),
+                                   el_range=np.linspace(-90, 90, 5), scatter_points=sc, wavelength=CUDA_MODEL_LAMBDA,
+                                   farfield_distance=5.0, beta=2 * np.pi / CUDA_MODEL_LAMBDA, cuda=True, **kw)
+    assert rel_err(et, d[f"{label}_theta"]) < 1e-5 and rel_err(ep, d[f"{label}_phi"]) < 1e-5
     _no_device_errors()
 

@@ -446,13 +446,16 @@ def test_frequency_domain_api():
     beta = 2 * np.pi / 0.04
     axis = np.array([1.0, 0, 0])
     Ex, Ey, Ez = FD.calculate_scattering(ap, sk, solid, axis, wavelength=0.04, beta=beta, cuda=True)
-    Eo = O.sink_field(src, np.tile(axis * 0.5, (5, 1)), snk, snk_n, 0.0, beta, tris12=O.pack_triangles(v, f))
+    # the CUDA engine's em bindings take beta as float32
+    Eo = O.sink_field(src, np.tile(axis * 0.5, (5, 1)), snk, snk_n, 0.0, float(np.float32(beta)),
+                      tris12=O.pack_triangles(v, f))
     assert rel_err(np.stack([Ex, Ey, Ez], 1), Eo) < FIELD_TOL
-    Sx, Sy, Sz = FD.calculate_scattering(ap, sk, solid, axis, wavelength=0.04, beta=beta, elements=True)
+    Sx, Sy, Sz = FD.calculate_scattering(ap, sk, solid, axis, wavelength=0.04, beta=beta, elements=True, cuda=True)
     assert Sx.shape == (5, 60)
     assert rel_err(np.stack([Sx, Sy, Sz], -1).sum(0), Eo) < FIELD_TOL
     et, ep = FD.calculate_farfield(ap, solid, axis, az_range=np.linspace(-180, 180, 9),
-                                   el_range=np.linspace(-90, 90, 5), wavelength=0.04, farfield_distance=5.0, beta=beta)
+                                   el_range=np.linspace(-90, 90, 5), wavelength=0.04, farfield_distance=5.0, beta=beta,
+                                   cuda=True)
     assert et.shape == (45,) and np.isfinite(et).all() and np.isfinite(ep).all()
 
 
@@ -636,13 +639,13 @@ def test_scene_cache_reuses_device_grid():
     sk = Mesh(snk, point_data={"Normals": snk_n})
     axis = np.array([0.0, 1.0, 0.0])
     h0, m0 = A.cache_stats["hits"], A.cache_stats["misses"]
-    first = FD.calculate_scattering(ap, sk, Mesh(v, [("triangle", f)]), axis, beta=150.0)
-    again = FD.calculate_scattering(ap, sk, Mesh(v.copy(), [("triangle", f.copy())]), axis, beta=150.0)
+    first = FD.calculate_scattering(ap, sk, Mesh(v, [("triangle", f)]), axis, beta=150.0, cuda=True)
+    again = FD.calculate_scattering(ap, sk, Mesh(v.copy(), [("triangle", f.copy())]), axis, beta=150.0, cuda=True)
     assert A.cache_stats["misses"] == m0 + 1 and A.cache_stats["hits"] == h0 + 1
     for x, y in zip(first, again):
         assert np.array_equal(x, y)
     v2 = v.copy()
     v2[0, 0] += 0.01
-    FD.calculate_scattering(ap, sk, Mesh(v2, [("triangle", f)]), axis, beta=150.0)
+    FD.calculate_scattering(ap, sk, Mesh(v2, [("triangle", f)]), axis, beta=150.0, cuda=True)
     assert A.cache_stats["misses"] == m0 + 2
     _no_device_errors()
