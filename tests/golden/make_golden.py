@@ -30,7 +30,8 @@ Fixtures:
                           two wavelengths and with magnetic sources; TimeDomainv3 (:2910-3170) on a
                           one-block path list, with 400 and with 120 samples; and the model-level
                           calculate_scattering(cuda=False) (lyceanem/models/frequency_domain.py:
-                          267-718) for direct, one- and two-bounce paths.
+                          267-718) for direct, one- and two-bounce paths; the time-domain model
+                          (lyceanem/models/time_domain.py) on a one-block scene.
   cuda_model.npz          the reference's CUDA-engine model layer (calculate_scattering(cuda=True),
                           calculate_scattering_cuda, Tile_acceleration_structure.calculate_scattering,
                           calculate_farfield; lyceanem/models/frequency_domain.py:94-264, 719-926,
@@ -345,6 +346,31 @@ def numba_engine():
             key = f"model_{name}_{scattering}{int(los)}{int(elements)}{int(project)}"
             out[key] = np.stack(res, -1)
             print("  calculate_scattering(cuda=False)", key, out[key].shape)
+    # the time-domain model (lyceanem/models/time_domain.py:14-...) on scene t (its path lists stay within one
+    # thread block of the time kernel, whose wake time is synchronised only within a block)
+    import lyceanem.models.time_domain as TDM
+    sc = scenes["t"]
+    n_src = sc["src"].shape[0]
+    exc = np.sin(np.linspace(0, 6 * np.pi, 40)) * np.hanning(40)
+    solid = meshio.Mesh(sc["verts"], [("triangle", sc["faces"])])
+    for label, kw in (("s0", dict(scattering=0, project_vectors=False)), ("s1", dict(scattering=1, project_vectors=False)),
+                      ("s1_project", dict(scattering=1)), ("s1_elements", dict(scattering=1, elements=True,
+                                                                                project_vectors=False))):
+        ap = meshio.Mesh(sc["src"], [], point_data={"Normals": np.tile([[0, 0, 1.0]], (n_src, 1)),
+                                                   "Area": np.full(n_src, 0.25)})
+        sk = meshio.Mesh(sc["snk"], [], point_data={"Normals": sc["snk_n"]})
+        sp = meshio.Mesh(sc["scat"], [], point_data={"Normals": sc["scat_n"]})
+        try:
+            res = TDM.calculate_scattering(ap, sk, exc, solid, np.array([1.0, 0.0, 0.0]), scatter_points=sp,
+                                           wavelength=0.05, sampling_freq=20e9, num_samples=400, los=True,
+                                           beta=2 * np.pi / 0.05, **kw)
+        except TypeError as e:  # a reference call path that raises is recorded as such
+            print("  time_domain.calculate_scattering", label, "raises TypeError:", e)
+            out[f"td_{label}_raises"] = np.array(str(e))
+            continue
+        out[f"td_{label}"] = np.stack(res[:3], -1)
+        out[f"td_{label}_wake"] = np.asarray(res[3], np.float64)
+        print("  time_domain.calculate_scattering", label, out[f"td_{label}"].shape, np.asarray(res[3]))
     # per-path products: (case, wavelength, magnetic sources)
     alpha = 0.02
     for key, lam, mag in (("a2los", 0.5, 0), ("a2los", 0.05, 0), ("a2los", 0.5, 3), ("b3los", 0.5, 0)):

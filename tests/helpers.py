@@ -99,3 +99,10 @@ def cuda_model_golden():
     import os
     return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cuda_model.npz"))
 
+
+# time-domain model fixture cases on scene "t": (label, keyword arguments); areas 0.25, E axis +x, lambda 0.05 m,
+# 20 GHz sampling, 400 samples, the excitation of the TimeDomainv3 fixture
+NUMBA_TD_CASES = [("s0", dict(scattering=0, project_vectors=False)), ("s1", dict(scattering=1, project_vectors=False)),
+                  ("s1_project", dict(scattering=1)),
+                  ("s1_elements", dict(scattering=1, elements=True, project_vectors=False))]
+

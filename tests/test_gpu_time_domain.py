@@ -6,7 +6,7 @@ import torch
 
 from oracle import oracle as O
 
-from helpers import NUMBA_ALPHA, numba_golden, numba_golden_scene, random_scene, rel_err
+from helpers import NUMBA_ALPHA, NUMBA_TD_CASES, numba_golden, numba_golden_scene, random_scene, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -116,6 +116,31 @@ def test_timedomainv3_reference_golden():
                             d["time_excitation"], 20e9, 120, NUMBA_ALPHA, 2 * np.pi / 0.05)
     assert abs(wake - float(d["time_wake_short"])) < 1e-14
     assert rel_err(tm, d["time_map_short"]) < 1e-6
+    from lyceanem_gb300 import propagation as P
+    assert P.device_errors() == (0, 0)
+
+
+@pytest.mark.parametrize("label,kw", NUMBA_TD_CASES)
+def test_time_domain_model_reference_golden(label, kw):
+    """models.time_domain.calculate_scattering against the reference's own model function (fixture executed
+    from its source under the numba stand-in, one block of rows per time-kernel launch): wake time to the
+    reference's float32 path lengths, time series within 1e-5."""
+    from lyceanem_gb300.geometry import Mesh
+    from lyceanem_gb300.models import time_domain as TD
+    d = numba_golden()
+    src, snk, scat, v, f, _, _, _ = numba_golden_scene(d, "t")
+    n = src.shape[0]
+    ap = Mesh(src, point_data={"Normals": np.tile([[0, 0, 1.0]], (n, 1)), "Area": np.full(n, 0.25)})
+    sk = Mesh(snk, point_data={"Normals": d["t_snk_n"]})
+    sc = Mesh(scat, point_data={"Normals": d["t_scat_n"]})
+    out = TD.calculate_scattering(ap, sk, d["time_excitation"], Mesh(v, [("triangle", f)]), np.array([1.0, 0.0, 0.0]),
+                                  scatter_points=sc, wavelength=0.05, sampling_freq=20e9, num_samples=400, los=True,
+                                  beta=2 * np.pi / 0.05, **kw)
+    got = np.stack(out[:3], -1)
+    ref = d[f"td_{label}"]
+    assert got.shape == ref.shape
+    assert np.abs(np.asarray(out[3], np.float64).reshape(-1) - d[f"td_{label}_wake"].reshape(-1)).max() < 1e-14
+    assert rel_err(got, ref) < 1e-5
     from lyceanem_gb300 import propagation as P
     assert P.device_errors() == (0, 0)
 
