@@ -145,7 +145,8 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * lyceanem/src/raycasting.cuh:19-68 (cull = 1) or the numba engine's
  * lyceanem/raycasting/rayfunctions.py:37-104 (cull = 0, eps = 1e-7) against all
  * packed triangles (brute force, d_cell_start == NULL) or a grid from
- * lyem_grid_fill (d_cell_start, d_cell_tris and d_cell_box all given).  self_to_self = 0 reproduces the reference's skip of the pair
+ * lyem_grid_fill (d_cell_start, d_cell_tris and d_cell_box all given); eps, the determinant threshold, must be
+ * finite and not negative (LYEM_ERR_INVALID otherwise).  self_to_self = 0 reproduces the reference's skip of the pair
  * whose source index equals its sink index (lyceanem/src/raycasting_brute_force.cuh:27).
  * Replaces raycast_brute_force / raycast_tiles + set_values + points_to_rays
  * (lyceanem/src/raycasting_brute_force.cuh:68-88, raycasting_accelerated.cuh:458-482,
@@ -326,7 +327,7 @@ typedef struct lyem_batch_config {
     int32_t src_chunk;     /* sources per visibility item: 32 or 64 */
     int32_t blocks_per_sm; /* resident blocks per SM of the persistent launch, 0..8 (0: as many as fit) */
     int32_t cull;          /* back-face culling (the CUDA engine's rule) */
-    float eps;             /* determinant threshold of the ray-triangle test */
+    float eps;             /* determinant threshold of the ray-triangle test (finite, >= 0) */
     int32_t self_to_self;  /* 0: the pair (n, m) with equal indices is not tested (the reference default) */
     double alpha;          /* attenuation */
 } lyem_batch_config;

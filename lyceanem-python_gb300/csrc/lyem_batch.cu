@@ -453,7 +453,7 @@ bool config_ok(const lyem_batch_config* c) {
     if (!(c->freq_group == 1 || c->freq_group == 2 || c->freq_group == 4 || c->freq_group == 8)) return false;
     if (!(c->src_chunk == 32 || c->src_chunk == 64)) return false;
     if (c->blocks_per_sm < 0 || c->blocks_per_sm > 8) return false;
-    if (!(c->eps >= 0.f) || !isfinite(c->alpha)) return false;
+    if (!(c->eps >= 0.f) || !isfinite(c->eps) || !isfinite(c->alpha)) return false;
     return true;
 }
 

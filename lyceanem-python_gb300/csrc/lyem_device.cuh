@@ -135,6 +135,85 @@ __device__ __forceinline__ bool numba_tail(float A, float u, float v, float w, f
     return (t > two_eps) && (t < (double)len - two_eps);
 }
 
+// IEEE binary32 round-to-nearest operations usable on the host as well (the
+// host build is for tests of the decision logic below; compile host code with
+// -ffp-contract=off).
+namespace rn {
+__host__ __device__ __forceinline__ float mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ float add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+__host__ __device__ __forceinline__ float rcp(float a) {
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(a);
+#else
+    return 1.0f / a;
+#endif
+}
+}  // namespace rn
+
+// The culling test's decisions after the determinant, as the reference makes
+// them (lyceanem/src/raycasting.cuh:44-66): F = rn(1/A), U = rn(F u),
+// V = rn(F v), t = rn(F w); hit iff 0 <= U <= 1, V >= 0, rn(U + V) <= 1,
+// t > 2 eps and t < rn(len - 2 eps).
+__host__ __device__ __forceinline__ bool cull_tail_exact(float A, float u, float v, float w, float len, float eps) {
+    const float F = rn::rcp(A);
+    const float U = rn::mul(F, u);
+    if (U < 0.f || U > 1.f) return false;
+    const float V = rn::mul(F, v);
+    if (V < 0.f || rn::add(U, V) > 1.f) return false;
+    const float t = rn::mul(F, w);
+    const float two_eps = 2.f * eps;
+    return (t > two_eps) && (t < rn::sub(len, two_eps));
+}
+
+// The same decisions without the reciprocal where they are certain.  For A in
+// [2^-90, 2^90], F = rn(1/A) is within 2^-24 of 1/A, and each rounded product
+// within 2^-24 of its exact value, so (all margins at least 2^-19 against a
+// few units of 2^-24):
+//   u, v >= 0 and rn(u + v) <= rn(A (1 - 2^-19))  =>  U, V in [0, 1], rn(U + V) <= 1;
+//   rn(u + v) > ahi = rn(A + A 2^-19) (u, v past their guard bands)  =>  rn(U + V) > 1;
+//   w <= 0  =>  t <= 0: a miss;
+//   w > rn(A max(4 eps, 2^-30))  =>  t > 2 eps;
+//   w < rn(rn(L (1 - 2^-18)) A)  =>  t < L,   w > rn(rn(L (1 + 2^-18)) A)  =>  t > L,
+// with L = rn(len - 2 eps) in [2^-20, 2^30] (no product over- or underflows).
+// Everything else (pairs within about 2^-19 of an edge of the test, or of the
+// ends of the segment) takes the reference's own sequence, so the result is
+// the reference's bit for bit.  ahi is the guard-band bound the caller used
+// for u and v.
+__host__ __device__ __forceinline__ bool cull_tail(float A, float u, float v, float w, float len, float eps,
+                                                   float ahi) {
+    const float two_eps = 2.f * eps;
+    const float L = rn::sub(len, two_eps);
+    if (A >= 0x1p-90f && A <= 0x1p90f && L >= 0x1p-20f && L <= 0x1p30f) {
+        const float uv = rn::add(u, v);
+        const float Lhi = rn::mul(rn::mul(L, 1.f + 0x1p-18f), A);
+        if (uv > ahi || w <= 0.f || w > Lhi) return false;
+        const float alo = rn::mul(A, 1.f - 0x1p-19f);
+        const float Llo = rn::mul(rn::mul(L, 1.f - 0x1p-18f), A);
+        const float b4 = rn::mul(A, fmaxf(rn::mul(4.f, eps), 0x1p-30f));
+        if (u >= 0.f && v >= 0.f && uv <= alo && w > b4 && w < Llo) return true;
+    }
+    return cull_tail_exact(A, u, v, w, len, eps);
+}
+
 // hit() with the per-source quantities precomputed.
 template <bool CULL>
 __device__ __forceinline__ bool hit_pre(const Ray& r, const TriPre& p, float eps) {
@@ -182,20 +261,18 @@ __device__ __forceinline__ bool hit_full(const Ray& r, float ox, float oy, float
         if (ratio_negative(v, A)) return false;
         return numba_tail(A, u, v, __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx))), r.len, eps);
     }
-    if (outside_unit(u, A)) return false;
-    float F = __frcp_rn(A);
-    float U = __fmul_rn(F, u);
-    if (U < 0.f || U > 1.f) return false;
+    // A >= eps >= 0 (the entry points reject a negative eps): outside_unit's
+    // guard band with A's sign known (A = -0 or +0: every u other than zero is
+    // a miss there, as the reference's infinite F makes it)
+    const float aneg = __fmul_rn(A, -0x1p-20f), ahi = __fmaf_rn(A, 0x1p-19f, A);
+    if (u < aneg || u > ahi) return false;
     float qx = __fmaf_rn(ty, e1.z, -__fmul_rn(tz, e1.y));
     float qy = __fmaf_rn(tz, e1.x, -__fmul_rn(tx, e1.z));
     float qz = __fmaf_rn(tx, e1.y, -__fmul_rn(ty, e1.x));
     const float v = __fmaf_rn(r.dz, qz, __fmaf_rn(r.dy, qy, __fmul_rn(r.dx, qx)));
-    if (outside_unit(v, A)) return false;
-    float V = __fmul_rn(F, v);
-    if (V < 0.f || __fadd_rn(U, V) > 1.f) return false;
-    float t = __fmul_rn(F, __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx))));
-    const float two_eps = 2.f * eps;
-    return (t > two_eps) && (t < __fsub_rn(r.len, two_eps));
+    if (v < aneg || v > ahi) return false;
+    const float w = __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx)));
+    return cull_tail(A, u, v, w, r.len, eps, ahi);
 }
 
 // Path length in FP64 from the FP32 end points: the coordinate differences are
