@@ -378,7 +378,8 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
     if (m_ok) {
         ex = p.snk_pos[3 * m]; ey = p.snk_pos[3 * m + 1]; ez = p.snk_pos[3 * m + 2];
     }
-    unsigned long long blocked = 0, tests = 0;
+    unsigned long long blocked = 0;
+    unsigned int tests = 0;  // per lane: at most 64 rays, so the count stays far below 2^32
     Walk w;
     if (MODE == kTwoPhase16 || MODE == kTwoPhase12) {
         __shared__ int s_hint[kGridMaxChunk];

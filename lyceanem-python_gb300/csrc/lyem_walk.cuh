@@ -20,28 +20,30 @@ struct Walk {
 };
 
 // True when the segment certainly misses box [lo, hi]: slab test over the
-// parameter range [0, len] (a cell's own range is a part of it); an axis the
-// segment is parallel to only checks the origin coordinate.  The computed slab
-// parameters carry relative errors of a few units of 2^-24, so the box counts
-// as missed only when the entry parameter exceeds the exit parameter by more
-// than 2^-19 of it; NaN parameters never make a miss.
+// parameter range [0, len] (a cell's own range is a part of it).  The computed
+// slab parameters carry relative errors of a few units of 2^-24, so the box
+// counts as missed only when the entry parameter exceeds the exit parameter by
+// more than 2^-19 of it; NaN parameters never make a miss.  An axis the segment
+// is parallel to (direction component 0) has the finite stand-in +-2^100 for
+// 1/D (walk_setup), so its slab parameters are 0 or of magnitude 2^100 |L - O|:
+// outside the slab the box is missed, inside it the slab cuts nothing, and a
+// segment within about 2^-100 t of a face can be counted as missing the box.
+// That is safe: a box is the union of its triangles' boxes padded by `pad`
+// (clipped to the cell widened by two pads), so every hit point lies at least
+// a pad inside it, and 2^-100 t is far below any pad.
 __device__ __forceinline__ bool box_missed(const Walk& w, float4 lo, float4 hi) {
-    const float kInf = __int_as_float(0x7f800000);
     float tmin = 0.f, tmax = w.r.len;
-    bool out = false;
-#define LYEM_BOX(D, O, INV, L, H)                                     \
+#define LYEM_BOX(O, INV, L, H)                                        \
     {                                                                 \
-        const float ta = D != 0.f ? (L - O) * INV : -kInf;            \
-        const float tb = D != 0.f ? (H - O) * INV : kInf;             \
+        const float ta = (L - O) * INV, tb = (H - O) * INV;           \
         tmin = fmaxf(tmin, fminf(ta, tb));                            \
         tmax = fminf(tmax, fmaxf(ta, tb));                            \
-        out |= D == 0.f && (O < L || O > H);                          \
     }
-    LYEM_BOX(w.r.dx, w.ox, w.ix, lo.x, hi.x)
-    LYEM_BOX(w.r.dy, w.oy, w.iy, lo.y, hi.y)
-    LYEM_BOX(w.r.dz, w.oz, w.iz, lo.z, hi.z)
+    LYEM_BOX(w.ox, w.ix, lo.x, hi.x)
+    LYEM_BOX(w.oy, w.iy, lo.y, hi.y)
+    LYEM_BOX(w.oz, w.iz, lo.z, hi.z)
 #undef LYEM_BOX
-    return out || __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax;
+    return __fmul_rn(tmin, 1.f - 0x1p-19f) > tmax;
 }
 
 // Enters cell c: the ref range of the children whose boxes the segment may
@@ -81,7 +83,7 @@ __device__ __forceinline__ bool walk_setup(const GP& p, Walk& w) {
     bool miss = false;
 #define LYEM_SLAB(D, O, G0, G1, INV)                       \
     if (D == 0.f) {                                        \
-        INV = 0.f;                                         \
+        INV = copysignf(0x1p100f, D);                      \
         if (O < G0 || O > G1) miss = true;                 \
     } else {                                               \
         INV = 1.0f / D;                                    \
@@ -186,7 +188,7 @@ __device__ __forceinline__ bool walk_setup_from(const GP& p, Walk& w, float from
     bool miss = false;
 #define LYEM_SLAB(D, O, G0, G1, INV)                       \
     if (D == 0.f) {                                        \
-        INV = 0.f;                                         \
+        INV = copysignf(0x1p100f, D);                      \
         if (O < G0 || O > G1) miss = true;                 \
     } else {                                               \
         INV = 1.0f / D;                                    \
