@@ -209,19 +209,28 @@ __device__ __forceinline__ bool walk_setup_from(const GP& p, Walk& w, float from
     return true;
 }
 
+// Parameters of the next crossing of a cell boundary along each axis (the
+// boundary ahead of the current cell, recomputed from the cell index; +inf for
+// an axis the segment is parallel to).
+template <class GP>
+__device__ __forceinline__ void next_crossings(const GP& p, const Walk& w, float& tx, float& ty, float& tz) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float cell = p.cell;
+    tx = (p.g0[0] + (float)(w.cx + (w.r.dx > 0.f ? 1 : 0)) * cell - w.ox) * w.ix;
+    ty = (p.g0[1] + (float)(w.cy + (w.r.dy > 0.f ? 1 : 0)) * cell - w.oy) * w.iy;
+    tz = (p.g0[2] + (float)(w.cz + (w.r.dz > 0.f ? 1 : 0)) * cell - w.oz) * w.iz;
+    if (w.r.dx == 0.f) tx = kInf;
+    if (w.r.dy == 0.f) ty = kInf;
+    if (w.r.dz == 0.f) tz = kInf;
+}
+
 // Crosses the nearest cell boundary unless the crossing lies at or beyond
 // parameter `stop`: 0 = the segment or the grid ends there, 1 = the next cell
 // was entered, 2 = stopped before a crossing at or beyond `stop`.
 template <class GP>
 __device__ __forceinline__ int walk_step_until(const GP& p, Walk& w, float stop, unsigned int* err) {
-    const float kInf = __int_as_float(0x7f800000);
-    const float cell = p.cell;
-    const float tx = w.r.dx > 0.f ? (p.g0[0] + (float)(w.cx + 1) * cell - w.ox) * w.ix
-                                  : (w.r.dx < 0.f ? (p.g0[0] + (float)w.cx * cell - w.ox) * w.ix : kInf);
-    const float ty = w.r.dy > 0.f ? (p.g0[1] + (float)(w.cy + 1) * cell - w.oy) * w.iy
-                                  : (w.r.dy < 0.f ? (p.g0[1] + (float)w.cy * cell - w.oy) * w.iy : kInf);
-    const float tz = w.r.dz > 0.f ? (p.g0[2] + (float)(w.cz + 1) * cell - w.oz) * w.iz
-                                  : (w.r.dz < 0.f ? (p.g0[2] + (float)w.cz * cell - w.oz) * w.iz : kInf);
+    float tx, ty, tz;
+    next_crossings(p, w, tx, ty, tz);
     const float tc = fminf(tx, fminf(ty, tz));
     if (tc > w.t1) return 0;
     if (tc >= stop) return 2;
@@ -248,14 +257,8 @@ __device__ __forceinline__ int walk_step_until(const GP& p, Walk& w, float stop,
 // Crosses the nearest cell boundary; false when the segment or the grid ends there.
 template <class GP>
 __device__ __forceinline__ bool walk_step(const GP& p, Walk& w, unsigned int* err) {
-    const float kInf = __int_as_float(0x7f800000);
-    const float cell = p.cell;
-    const float tx = w.r.dx > 0.f ? (p.g0[0] + (float)(w.cx + 1) * cell - w.ox) * w.ix
-                                  : (w.r.dx < 0.f ? (p.g0[0] + (float)w.cx * cell - w.ox) * w.ix : kInf);
-    const float ty = w.r.dy > 0.f ? (p.g0[1] + (float)(w.cy + 1) * cell - w.oy) * w.iy
-                                  : (w.r.dy < 0.f ? (p.g0[1] + (float)w.cy * cell - w.oy) * w.iy : kInf);
-    const float tz = w.r.dz > 0.f ? (p.g0[2] + (float)(w.cz + 1) * cell - w.oz) * w.iz
-                                  : (w.r.dz < 0.f ? (p.g0[2] + (float)w.cz * cell - w.oz) * w.iz : kInf);
+    float tx, ty, tz;
+    next_crossings(p, w, tx, ty, tz);
     bool done;
     if (tx <= ty && tx <= tz) {
         w.cx += w.r.dx > 0.f ? 1 : -1;
