@@ -323,7 +323,8 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     }
     if (!d_src_pos || !d_src_E || !d_snk_pos || !d_snk_nrm) return LYEM_ERR_INVALID;
     if (!(eps >= 0.f) || !isfinite(eps)) return LYEM_ERR_INVALID;  // the culling test relies on A >= eps >= 0
-    if (n_src > (1LL << 31) || n_snk > (1LL << 31)) return LYEM_ERR_OVERFLOW;
+    // the stage kernels index sources and sinks in 32 bits
+    if (n_src >= (1LL << 31) - 256 || n_snk >= (1LL << 31) - 256) return LYEM_ERR_OVERFLOW;
     if (use_grid) {
         if (!d_cell_tris || !aligned16(d_cell_tris) || !d_cell_box || !aligned16(d_cell_box) ||
             !valid_grid(grid_origin3, grid_cell, grid_dims3))

@@ -362,21 +362,27 @@ constexpr int kLockstep16 = 4;
 constexpr int kTwoPhase16 = 5;
 constexpr int kTwoPhase12 = 6;
 
-template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, int MODE>
+// COUNT = false (only with the default schedule, when the caller asks for no
+// counters) leaves the per-test counting out of the walk: one instruction and
+// one register less in the innermost loop (scatter->sink stage of the 28 GHz
+// scene 448 -> 440 ms).
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, int MODE, bool COUNT = true>
 __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == kLockstep12 || MODE == kTwoPhase12) ? 12 : (MODE == kLockstep16 || MODE == kTwoPhase16) ? 16 : 1) grid_stage_kernel(const StageParams p) {
+    // 32-bit indices (fewer live registers in the walk): the entry point keeps
+    // n_src and n_snk below 2^31 - 256
     const int tid = threadIdx.x;
-    const long long ms = (long long)blockIdx.x * kThreads + tid;
+    const int ms = (int)blockIdx.x * kThreads + tid;
     const bool m_ok = ms < p.n_snk;
-    const long long m = m_ok ? (p.snk_order ? (long long)p.snk_order[ms] : ms) : 0;
-    const long long n0 = (p.chunk_base + (long long)blockIdx.y) * p.src_chunk;
-    const long long rem = p.n_src - n0;
-    const int nsrc = (int)(rem < p.src_chunk ? rem : p.src_chunk);
-    auto src_index = [&](int s) -> long long {
-        return p.src_order ? (long long)p.src_order[n0 + s] : n0 + s;
+    const int m = m_ok ? (p.snk_order ? p.snk_order[ms] : ms) : 0;
+    const int n0 = (int)((p.chunk_base + (long long)blockIdx.y) * p.src_chunk);
+    const int rem = (int)p.n_src - n0;
+    const int nsrc = rem < p.src_chunk ? rem : p.src_chunk;
+    auto src_index = [&](int s) -> int {
+        return p.src_order ? p.src_order[n0 + s] : n0 + s;
     };
     float ex = 0.f, ey = 0.f, ez = 0.f;
     if (m_ok) {
-        ex = p.snk_pos[3 * m]; ey = p.snk_pos[3 * m + 1]; ez = p.snk_pos[3 * m + 2];
+        ex = p.snk_pos[3 * (long long)m]; ey = p.snk_pos[3 * (long long)m + 1]; ez = p.snk_pos[3 * (long long)m + 2];
     }
     unsigned long long blocked = 0;
     unsigned int tests = 0;  // per lane: at most 64 rays, so the count stays far below 2^32
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
         unsigned short* queue = s_queue + (size_t)warp * p.src_chunk * 32;
         s_blk[warp][lane] = 0ull;
         for (int s = warp; s < nsrc; s += kThreads / 32) {
-            const float* so = p.src_pos + 3 * src_index(s);
+            const float* so = p.src_pos + 3 * (long long)src_index(s);
             const int h = warp_nearest_ref(p, so[0], so[1], so[2]);
             if (lane == 0) s_hint[s] = h;
         }
@@ -398,10 +404,10 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
         const unsigned full = 0xffffffffu;
         int count = 0;  // the same in every lane of the warp
         for (int s = 0; s < nsrc; ++s) {
-            const long long n = src_index(s);
+            const int n = src_index(s);
             bool far = false;
             if (m_ok && !(p.skip_diag && n == m)) {
-                const float* so = p.src_pos + 3 * n;
+                const float* so = p.src_pos + 3 * (long long)n;
                 walk_ray<CULL>(w, so[0], so[1], so[2], ex, ey, ez);
                 const int hint = s_hint[s];
                 bool hit = false;
@@ -438,7 +444,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
             const float qx = __shfl_sync(full, ex, owner), qy = __shfl_sync(full, ey, owner),
                         qz = __shfl_sync(full, ez, owner);
             if (has) {
-                const float* so = p.src_pos + 3 * src_index(s);
+                const float* so = p.src_pos + 3 * (long long)src_index(s);
                 walk_ray<CULL>(w, so[0], so[1], so[2], qx, qy, qz);
                 bool hit = false;
                 if (walk_setup_from(p, w, near)) {
@@ -460,26 +466,26 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
         // tried first by every ray from that source
         __shared__ int s_hint[kGridMaxChunk];
         for (int s = tid >> 5; s < nsrc; s += kThreads / 32) {
-            const float* so = p.src_pos + 3 * src_index(s);
+            const float* so = p.src_pos + 3 * (long long)src_index(s);
             const int h = warp_nearest_ref(p, so[0], so[1], so[2]);
             if ((tid & 31) == 0) s_hint[s] = h;
         }
         __syncthreads();
         for (int s = 0; s < nsrc; ++s) {
-            const long long n = src_index(s);
+            const int n = src_index(s);
             if (!m_ok || (p.skip_diag && n == m)) continue;
-            const float* so = p.src_pos + 3 * n;
+            const float* so = p.src_pos + 3 * (long long)n;
             walk_ray<CULL>(w, so[0], so[1], so[2], ex, ey, ez);
             const int hint = s_hint[s];
             bool hit = false;
             if (hint >= 0) {  // a hit on any triangle blocks the segment, walked or not
-                ++tests;
+                if (COUNT) ++tests;
                 hit = walk_test_ref<CULL>(p, w, hint);
             }
             if (!hit && !walk_setup(p, w)) continue;
             while (!hit) {
                 while (w.q < w.q1) {
-                    ++tests;
+                    if (COUNT) ++tests;
                     if (walk_test<CULL>(p, w)) { hit = true; break; }
                 }
                 if (hit || !walk_step(p, w, &g_device_error)) break;
@@ -492,9 +498,9 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
         // next source of this lane that needs a walk (untested and off-grid rays are visible)
         auto refill = [&]() {
             while (++s < nsrc) {
-                const long long n = src_index(s);
+                const int n = src_index(s);
                 if (p.skip_diag && n == m) continue;
-                const float* so = p.src_pos + 3 * n;
+                const float* so = p.src_pos + 3 * (long long)n;
                 if (walk_begin<CULL>(p, w, so[0], so[1], so[2], ex, ey, ez)) { has = true; return; }
             }
         };
@@ -521,15 +527,15 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
 
     float nx = 0.f, ny = 0.f, nz = 0.f;
     if (m_ok) {
-        nx = p.snk_nrm[3 * m]; ny = p.snk_nrm[3 * m + 1]; nz = p.snk_nrm[3 * m + 2];
+        nx = p.snk_nrm[3 * (long long)m]; ny = p.snk_nrm[3 * (long long)m + 1]; nz = p.snk_nrm[3 * (long long)m + 2];
     }
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     unsigned long long vis_count = 0;
     for (int k = 0; k < nsrc; ++k) {
-        const long long n = src_index(k);
+        const int n = src_index(k);
         const bool vis = m_ok && !((blocked >> k) & 1ull);
         record_visibility<MASK_OUT>(p, n, m, ms, vis);
-        const float* so = p.src_pos + 3 * n;
+        const float* so = p.src_pos + 3 * (long long)n;
         pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, m_ok, vis, so[0], so[1], so[2], ex, ey, ez, nx, ny, nz, acc);
         vis_count += vis;
     }
@@ -562,8 +568,13 @@ static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase16><<<grid, kThreads, qbytes, stream>>>(p);
                 else
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase12><<<grid, kThreads, qbytes, stream>>>(p);
-            } else if (p.refill_lanes == -16)
-                grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);
+            } else if (p.refill_lanes == -16) {
+                if (p.counters)
+                    grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);
+                else
+                    grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16, false>
+                        <<<grid, kThreads, 0, stream>>>(p);
+            }
             else if (p.refill_lanes == -12)
                 grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep12><<<grid, kThreads, 0, stream>>>(p);
             else if (p.refill_lanes == -10)

@@ -288,7 +288,8 @@ def test_bounce_config_full_geometry_slice():
 def test_grid_schedules_bit_identical_full_geometry(traversal):
     """Every grid schedule (lockstep capped and uncapped; two phases split at 2, 4 and 3 cells) gives the
     oracle's masks and the same sink field on the full 28 GHz geometry (slice of sinks and scatter points,
-    the benchmarked processing orders), for the array-to-sink and scatter-to-sink stages."""
+    the benchmarked processing orders), for the array-to-sink and scatter-to-sink stages, with and without
+    the test counters."""
     from lyceanem_gb300 import scenes
     P = _P()
     s = scenes.bounce_scene()
@@ -308,6 +309,11 @@ def test_grid_schedules_bit_identical_full_geometry(traversal):
         r = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=traversal, **kw)
         assert np.array_equal(r.mask().cpu().numpy(), og.mask(a, b))
         assert torch.equal(r.sink, ref.sink)
+        # with counters (the default schedule then runs its counting variant): same results
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        rc = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=traversal, counters=cnt, **kw)
+        assert torch.equal(rc.mask_bits, r.mask_bits) and torch.equal(rc.sink, r.sink)
+        assert int(cnt[0]) == int(r.mask().sum()) and int(cnt[1]) > 0
     _no_device_errors()
 
 
