@@ -101,9 +101,9 @@ LYEM_API int lyem_grid_count(const float *d_tris, int64_t n_tris, const float *o
  * by cell (stable, so triangles are ascending within a cell), writes the cell
  * ranges d_cell_start[ncells+1], the triangles in cell order
  * d_cell_tris[n_refs,12] and the traversal's cell table d_cell_box[ncells,16]
- * (16-byte aligned).  Within a cell the triangles are split at the cell's
- * centre (along the axis of largest centroid spread) into child A then child
- * B, each in ascending triangle order; the record is (loA.xyz, first ref,
+ * (16-byte aligned).  Within a cell the triangles are split by the axis-aligned
+ * plane (k/8 of the cell on one axis, k = 1..7) of least surface-area cost
+ * into child A (centroid below) then child B, each in ascending triangle order; the record is (loA.xyz, first ref,
  * hiA.xyz, first ref of B, loB.xyz, first ref of B, hiB.xyz, end ref), refs
  * stored as int32 bits, each [lo, hi] the box of the child's triangles (padded
  * as for the binning) within the cell widened by two pads; a segment that

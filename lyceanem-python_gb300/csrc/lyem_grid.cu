@@ -330,8 +330,8 @@ __global__ void gather_tris_kernel(const float4* __restrict__ tris, const int* _
 }
 
 // Cell table of the traversal and the cell-ordered triangles, one thread per
-// cell.  A cell's triangles are split at the cell's centre along the axis of
-// largest centroid spread into two children, A (centroid below) then B, each
+// cell.  A cell's triangles are split by an axis-aligned plane (surface-area
+// cost, below) into two children, A (centroid below) then B, each
 // kept in the (ascending) triangle order of the sorted refs, and the record of
 // cell c is four float4:
 //   (loA.xyz, first ref) (hiA.xyz, first ref of B) (loB.xyz, first ref of B) (hiB.xyz, end ref)
@@ -367,29 +367,55 @@ __global__ void cell_fill_kernel(BinSpec b, const float4* __restrict__ tris, con
         const int q0 = cell_start[c], q1 = cell_start[c + 1];
         const long long iz = c / plane, rem = c - iz * plane, iy = rem / b.dims[0], ix = rem - iy * b.dims[0];
         const float ci[3] = {(float)ix, (float)iy, (float)iz};
-        // split axis: largest spread of the centroids; split plane: the cell's centre on it
-        float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int r = q0; r < q1; ++r) {
-            const float4* t = tris + 3 * (long long)vals[r];
-            const float4 v0 = t[0], e1 = t[1], e2 = t[2];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float x = tri_centroid(v0, e1, e2, k);
-                cmin[k] = fminf(cmin[k], x);
-                cmax[k] = fmaxf(cmax[k], x);
-            }
-        }
+        // split: of the planes at k/8 of the cell (k = 1..7) on each axis, the one
+        // with the least surface-area cost (the clipped child boxes' areas times
+        // their triangle counts, a ray's chance of entering a box being about
+        // proportional to its area); a triangle goes to child A when its centroid
+        // lies below the plane.  Visibility does not depend on the split.
         int ax = 0;
-        float spread = -1.f;
+        float mid = b.org[0] + (ci[0] + 0.5f) * b.cell;
+        if (q1 - q0 > 1) {
+            float best = INFINITY;
+            for (int a = 0; a < 3; ++a) {
+                for (int k = 1; k < 8; ++k) {
+                    const float plane = b.org[a] + (ci[a] + 0.125f * (float)k) * b.cell;
+                    float lo[2][3], hi[2][3];
+                    int n[2] = {0, 0};
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float d = cmax[k] - cmin[k];
-            if (d > spread) {
-                spread = d;
-                ax = k;
+                    for (int h = 0; h < 2; ++h)
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            lo[h][d] = INFINITY;
+                            hi[h][d] = -INFINITY;
+                        }
+                    for (int r = q0; r < q1; ++r) {
+                        const float4* t = tris + 3 * (long long)vals[r];
+                        const float4 v0 = t[0], e1 = t[1], e2 = t[2];
+                        const int h = tri_centroid(v0, e1, e2, a) < plane ? 0 : 1;
+                        ++n[h];
+                        tri_box(b, v0, e1, e2, lo[h], hi[h]);
+                    }
+                    float cost = 0.f;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (!n[h]) continue;
+                        float ext[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            const float c0 = b.org[d] + ci[d] * b.cell;
+                            ext[d] = fmaxf(fminf(hi[h][d], c0 + b.cell + 2.f * b.pad) -
+                                               fmaxf(lo[h][d], c0 - 2.f * b.pad), 0.f);
+                        }
+                        cost += (ext[0] * ext[1] + ext[1] * ext[2] + ext[2] * ext[0]) * (float)n[h];
+                    }
+                    if (cost < best) {
+                        best = cost;
+                        ax = a;
+                        mid = plane;
+                    }
+                }
             }
         }
-        const float mid = b.org[ax] + (ci[ax] + 0.5f) * b.cell;
         int na = 0;
         for (int r = q0; r < q1; ++r) {
             const float4* t = tris + 3 * (long long)vals[r];

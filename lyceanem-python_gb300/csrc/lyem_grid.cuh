@@ -33,7 +33,7 @@ cudaError_t grid_count(const BinSpec& b, const float4* tris, long long n_tris, i
 
 size_t grid_fill_workspace_bytes(long long n_refs, long long n_cells);
 // Also writes the traversal's cell table cell_box[4 * ncells] (3-D grids only):
-// per cell two children (its triangles split at the cell centre), each with the
+// per cell two children (its triangles split by a plane of least surface-area cost), each with the
 // union of its padded triangle boxes (the boxes the binning used) clipped to the
 // cell widened by two pads, and its ref range (see cell_fill_kernel).
 cudaError_t grid_fill(const BinSpec& b, const float4* tris, long long n_tris, const int* tri_offsets, long long n_refs,

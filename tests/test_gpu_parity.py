@@ -188,8 +188,9 @@ def test_grid_build_matches_cpu_binning():
     start = g.cell_start.cpu().numpy()
     ct = g.cell_tris.cpu().numpy()
     assert start[-1] == g.n_refs == sum(len(c) for c in cells)
-    # cell table: per cell child A (centroid below the cell centre on the axis of largest centroid spread) then
-    # child B, each in triangle order, with the box of its padded triangle boxes within the cell widened by 2 pads
+    # cell table: per cell child A (centroid below the split plane) then child B, each in triangle order, with the
+    # box of its padded triangle boxes within the cell widened by 2 pads; the split plane is the candidate (k/8 of
+    # the cell on one axis, k = 1..7) of least surface-area cost (clipped child boxes' areas times their counts)
     box = g.cell_box.cpu().numpy()
     refs = np.ascontiguousarray(box[:, [3, 7, 11, 15]]).view(np.int32)
     assert np.array_equal(refs[:, 0], start[:-1]) and np.array_equal(refs[:, 3], start[1:])
@@ -203,17 +204,34 @@ def test_grid_build_matches_cpu_binning():
             continue
         ix = np.array([c % g.dims[0], (c // g.dims[0]) % g.dims[1], c // (g.dims[0] * g.dims[1])])
         c0 = org + ix * np.float32(g.cell)
-        spread = cen[L].max(0) - cen[L].min(0)
-        ax = int(np.argmax(spread))
-        mid = org[ax] + (ix[ax] + 0.5) * g.cell
-        in_a = cen[L, ax] < mid
         got = ct[start[c]:start[c + 1]]
         na = refs[c, 1] - refs[c, 0]
         assert sorted(map(tuple, got.tolist())) == sorted(map(tuple, t[L].tolist())), c
-        # the split rule, where FP32 and FP64 centroids cannot disagree (clear axis, no centroid at the plane)
-        clear_axis = np.sort(spread)[-1] - np.sort(spread)[-2] > 1e-4 if len(L) > 1 else True
-        if clear_axis and np.all(np.abs(cen[L, ax] - mid) > 1e-5):
-            assert np.array_equal(got[:na], t[L[in_a]]) and np.array_equal(got[na:], t[L[~in_a]]), c
+        if len(L) > 1:
+            # the split is one of the candidates (no centroid within 1e-5 of its plane, where FP32 and FP64
+            # centroids could disagree), and its cost is the least of all candidates' to FP32 rounding
+            costs, match = [], []
+            for a in range(3):
+                for k in range(1, 8):
+                    plane = org[a] + (ix[a] + 0.125 * k) * g.cell
+                    in_a = cen[L, a] < plane
+                    cost = 0.0
+                    for sel in (in_a, ~in_a):
+                        if not sel.any():
+                            continue
+                        lo = np.maximum(vlo[L[sel]].min(0), c0 - 2 * pad).astype(np.float64)
+                        hi = np.minimum(vhi[L[sel]].max(0), c0 + np.float32(g.cell) + 2 * pad).astype(np.float64)
+                        e = np.maximum(hi - lo, 0.0)
+                        cost += (e[0] * e[1] + e[1] * e[2] + e[2] * e[0]) * sel.sum()
+                    costs.append(cost)
+                    clear = np.all(np.abs(cen[L, a] - plane) > 1e-5)
+                    match.append(clear and np.array_equal(got[:na], t[L[in_a]]) and np.array_equal(got[na:], t[L[~in_a]]))
+            if any(match):
+                best = min(cst for cst, mt in zip(costs, match) if mt)
+                assert best <= min(costs) * (1 + 1e-4) + 1e-12, c
+            else:  # only where a centroid lies at a candidate plane may no candidate reproduce the split
+                assert np.any([np.any(np.abs(cen[L, a] - (org[a] + (ix[a] + 0.125 * k) * g.cell)) <= 1e-5)
+                               for a in range(3) for k in range(1, 8)]), c
         for child, rows in ((0, got[:na]), (1, got[na:])):
             lo_b, hi_b = box[c, 8 * child:8 * child + 3], box[c, 8 * child + 4:8 * child + 7]
             if not len(rows):
