@@ -171,7 +171,8 @@ __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView
         ey = __ldg(kpos + 3 * ms + 1);
         ez = __ldg(kpos + 3 * ms + 2);
     }
-    unsigned long long vis = 0, tests = 0;
+    unsigned long long vis = 0;
+    unsigned int tests = 0;  // per lane: at most 64 rays, far below 2^32 tests
     Walk w;
     for (int s = 0; s < nsrc; ++s) {
         if (!ok) continue;
@@ -206,7 +207,7 @@ __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView
     }
     if (P.counters) {
         const unsigned long long v = warp_sum((unsigned long long)__popcll(vis));
-        const unsigned long long t = warp_sum(tests);
+        const unsigned long long t = warp_sum((unsigned long long)tests);
         if (lane == 0) {
             atomicAdd(P.counters + 4LL * scene + stage, v);
             atomicAdd(P.counters + 4LL * scene + 3, t);
