@@ -64,6 +64,11 @@ def test_device_entry_points_reject_bad_arguments_without_gpu_work():
     assert lib.lyem_em_bin_counts(None, 0, None, 0, 0, 1, 0.0, 1.0, 0.0, None) == 1
     out = np.zeros(1, np.int32)
     assert lib.lyem_em_bin_counts(None, 0, None, 0, 1, 1, 0.0, -1.0, 0.0, out.ctypes.data) == 1
+    # the culling test relies on a determinant threshold that is finite and not negative
+    d = ctypes.c_void_p(256)
+    for eps in (-1e-6, float("nan"), float("inf")):
+        assert lib.lyem_pair_stage(d, d, None, 4, d, d, 4, d, 1, None, None, None, None, 0.0, None, 0.0, 1.0, 0, 1,
+                                   eps, None, 0, None, None, None, None, None, None, None, 0, 0, None, 0, None) == 1
 
 
 def test_direction_order_argument_checks():
