@@ -17,6 +17,12 @@ count and rate are reported beside it.
 --impl reference times the CPU restatement of the same path (the reference has
 no CPU implementation; its only engines run on the GPU) on the host cores, on a
 bounded sample of the same workload, extrapolated stage by stage.
+
+Side legs of the default run, each reported in its own object of the JSON line
+(skipped with --no-<leg>): full-geometry parity against the oracle, the
+direct-path workload (brute force) with its roofline and parity, the
+mixed-precision beam sweep, the adjoint, the batched many-scene launch, the
+end-to-end call through the reference-shaped API, and the CPU baseline.
 """
 import argparse
 import json
@@ -87,6 +93,8 @@ def parse():
     ap.add_argument("--batched-cell-scale", type=float, default=0.0,
                     help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
+    ap.add_argument("--no-direct", action="store_true",
+                    help="skip the direct-path (8x8 array, brute force) leg of the bounce workload's run")
     ap.add_argument("--sweep-case", choices=["full", "small"], default="full",
                     help="small: the beam-sweep scene on a 4 deg sink grid (4,186 sinks; profiling case)")
     ap.add_argument("--src-chunk", type=int, default=0,
@@ -329,11 +337,31 @@ def run_ours(args, rank, world):
         res["adjoint"] = run_adjoint(args)
     if rank == 0 and world == 1 and not args.no_batched:
         res["batched"] = run_batched(args)
+    if rank == 0 and world == 1 and not args.no_direct and args.workload == "bounce":
+        res["direct"] = run_direct(args, rank, world)
     if rank == 0 and world == 1 and not args.no_e2e:
         res["e2e"] = run_e2e(args, s, paths)
     if rank == 0 and world == 1 and not args.no_cpu:
         res["cpu_baseline"] = cpu_baseline(args, s, paths)
     return res
+
+
+def run_direct(args, rank, world, steps=50, warmup=5):
+    """The direct-path workload (8x8 array at 10 GHz, 2,664 sinks at 10 m, 1,024 obstruction triangles, brute
+    force) timed the same way as the main workload (L2 flushed before every step, CUDA events), with its
+    roofline and its full-size parity against the oracle; a reported side leg of the default run."""
+    a = argparse.Namespace(**vars(args))
+    a.workload, a.steps, a.warmup = "direct", steps, warmup
+    a.no_e2e = a.no_cpu = a.no_sweep = a.no_adjoint = a.no_batched = a.no_direct = True
+    a.no_parity = False
+    sub = run_ours(a, rank, world)
+    r = sub["roofline"]
+    return {"workload": sub["config"]["workload"], "steps": steps, "warmup": warmup,
+            "ms_per_step": sub["ms_per_step"], "value": sub["value"], "unit": sub["unit"],
+            "roofline": {k: r[k] for k in ("bound", "kernel", "achieved", "peak", "unit", "frac", "tests_per_launch",
+                                            "ops_per_test", "traffic")},
+            "parity": {k: sub["parity"][k] for k in ("sample", "pairs", "mask_mismatches", "edge_pairs",
+                                                     "field_rel_err", "ok")}}
 
 
 def run_e2e(args, s, paths):
