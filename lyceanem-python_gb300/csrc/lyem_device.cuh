@@ -95,21 +95,15 @@ __device__ __forceinline__ bool det_rejects(float A, float eps) {
     return fabsf(A) < eps;
 }
 
-// Guard band of the barycentric checks.  With F = rn(1/A) (relative error at
-// most 2^-24), s = sign(A) and x the unscaled numerator (u = t.p or v = d.q):
-//   s*x < -|A| 2^-20          =>  rn(F*x) < -2^-21 < 0
-//   s*x > rn(|A| (1 + 2^-19))  =>  F*x > (1 + 2^-20)(1 - 2^-24) > 1 + 2^-21, so rn(F*x) > 1
+// Guard band of the barycentric checks (used by hit_full's culling test, where
+// A >= eps >= 0).  With F = rn(1/A) (relative error at most 2^-24) and x the
+// unscaled numerator (u = t.p or v = d.q):
+//   x < rn(A * -2^-20)          =>  rn(F*x) < -2^-21 < 0
+//   x > rn(A + A 2^-19)          =>  F*x > (1 + 2^-20)(1 - 2^-24) > 1 + 2^-21, so rn(F*x) > 1
 // so a test whose numerator lies there fails the reference's U (or V) check
 // without the reciprocal being formed; for V > 1, U + V > 1 follows as U >= 0.
-// Every other test takes the exact path, so results are unchanged.  NaN
-// numerators fail both comparisons and take the exact path.  Used by the grid
-// walk (scatter->sink stage of the 28 GHz scene 969 -> 953 ms); the brute
-// kernel's precomputed test measured faster without it.
-__device__ __forceinline__ bool outside_unit(float x, float A) {
-    const float sa = fabsf(A);
-    const float sx = A < 0.f ? -x : x;
-    return sx < __fmul_rn(sa, -0x1p-20f) || sx > __fmaf_rn(sa, 0x1p-19f, sa);
-}
+// With A = +-0 (eps = 0) F is infinite and every nonzero numerator fails there
+// as well.  NaN numerators fail both comparisons and go on to cull_tail.
 
 // The numba engine's decisions after the determinant (rayfunctions.py:55-100):
 // there F = 1.0 / A, U = F u, V = F v and t = F w are FP64 (the float64 literal
@@ -261,9 +255,9 @@ __device__ __forceinline__ bool hit_full(const Ray& r, float ox, float oy, float
         if (ratio_negative(v, A)) return false;
         return numba_tail(A, u, v, __fmaf_rn(e2.z, qz, __fmaf_rn(e2.y, qy, __fmul_rn(e2.x, qx))), r.len, eps);
     }
-    // A >= eps >= 0 (the entry points reject a negative eps): outside_unit's
-    // guard band with A's sign known (A = -0 or +0: every u other than zero is
-    // a miss there, as the reference's infinite F makes it)
+    // A >= eps >= 0 (the entry points reject a negative eps): the guard band
+    // above (A = -0 or +0: every u other than zero is a miss there, as the
+    // reference's infinite F makes it)
     const float aneg = __fmul_rn(A, -0x1p-20f), ahi = __fmaf_rn(A, 0x1p-19f, A);
     if (u < aneg || u > ahi) return false;
     float qx = __fmaf_rn(ty, e1.z, -__fmul_rn(tz, e1.y));
