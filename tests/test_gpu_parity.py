@@ -125,6 +125,28 @@ def test_grazing_rays_masks_bit_exact(eps):
     _no_device_errors()
 
 
+@pytest.mark.parametrize("scale,snk_r", [(1.0, 4.0), (1e3, 4e3), (1.0, 3e9), (3e-3, 12e-3)])
+def test_masks_bit_exact_across_scales(scale, snk_r):
+    """Scenes scaled by 1e3 and 3e-3, and sinks 3e9 m away (segment lengths beyond 2^30, where the culling
+    test's reciprocal-free decisions give way to the reference's own sequence): culled masks of the brute-force
+    kernel and of the grid walk bit-exact to the oracle."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(41, n_src=24, n_snk=300, n_tris=500, box=1.0)
+    src = (src.astype(np.float64) * scale).astype(np.float32)
+    v = (v.astype(np.float64) * scale).astype(np.float32)
+    snk = (snk_n.astype(np.float64) * -snk_r).astype(np.float32)
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f), cull=True, eps=1e-6)
+    assert 0 < om.sum() < om.size
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    rb = P.pair_stage(src, E, snk, snk_n, beta=1.0, tris=tris, want_mask=True)
+    assert np.array_equal(rb.mask().cpu().numpy(), om)
+    for cell in (None, 0.4 * scale):
+        g = P.UniformGrid(tris, cell=cell)
+        r = P.pair_stage(src, E, snk, snk_n, beta=1.0, grid=g, want_mask=True)
+        assert np.array_equal(r.mask().cpu().numpy(), om), cell
+    _no_device_errors()
+
+
 @pytest.mark.parametrize("cull", [True, False])
 def test_lattice_scene_masks_bit_exact(cull):
     """Axis-aligned geometry on a lattice: axis-aligned quads lying on cell faces, sources and sinks on cell
