@@ -194,16 +194,19 @@ __host__ __device__ __forceinline__ bool cull_tail_exact(float A, float u, float
 // for u and v.
 __host__ __device__ __forceinline__ bool cull_tail(float A, float u, float v, float w, float len, float eps,
                                                    float ahi) {
-    const float two_eps = 2.f * eps;
-    const float L = rn::sub(len, two_eps);
-    if (A >= 0x1p-90f && A <= 0x1p90f && L >= 0x1p-20f && L <= 0x1p30f) {
+    if (A >= 0x1p-90f && A <= 0x1p90f) {
+        // the usual misses first (the line meets the plane outside the triangle, or behind the origin);
+        // neither claim depends on the segment's length
         const float uv = rn::add(u, v);
-        const float Lhi = rn::mul(rn::mul(L, 1.f + 0x1p-18f), A);
-        if (uv > ahi || w <= 0.f || w > Lhi) return false;
-        const float alo = rn::mul(A, 1.f - 0x1p-19f);
-        const float Llo = rn::mul(rn::mul(L, 1.f - 0x1p-18f), A);
-        const float b4 = rn::mul(A, fmaxf(rn::mul(4.f, eps), 0x1p-30f));
-        if (u >= 0.f && v >= 0.f && uv <= alo && w > b4 && w < Llo) return true;
+        if (uv > ahi || w <= 0.f) return false;
+        const float L = rn::sub(len, 2.f * eps);
+        if (L >= 0x1p-20f && L <= 0x1p30f) {
+            if (w > rn::mul(rn::mul(L, 1.f + 0x1p-18f), A)) return false;
+            const float alo = rn::mul(A, 1.f - 0x1p-19f);
+            const float Llo = rn::mul(rn::mul(L, 1.f - 0x1p-18f), A);
+            const float b4 = rn::mul(A, fmaxf(rn::mul(4.f, eps), 0x1p-30f));
+            if (u >= 0.f && v >= 0.f && uv <= alo && w > b4 && w < Llo) return true;
+        }
     }
     return cull_tail_exact(A, u, v, w, len, eps);
 }
@@ -225,14 +228,13 @@ __device__ __forceinline__ bool hit_pre(const Ray& r, const TriPre& p, float eps
         if (ratio_negative(v, A)) return false;
         return numba_tail(A, u, v, p.d.x, r.len, eps);
     }
-    float F = __frcp_rn(A);
-    float U = __fmul_rn(F, __fmaf_rn(p.c.x, pz, __fmaf_rn(p.b.w, py, __fmul_rn(p.b.z, px))));
-    if (U < 0.f || U > 1.f) return false;
-    float V = __fmul_rn(F, __fmaf_rn(r.dz, p.c.w, __fmaf_rn(r.dy, p.c.z, __fmul_rn(r.dx, p.c.y))));
-    if (V < 0.f || __fadd_rn(U, V) > 1.f) return false;
-    float t = __fmul_rn(F, p.d.x);
-    const float two_eps = 2.f * eps;
-    return (t > two_eps) && (t < __fsub_rn(r.len, two_eps));
+    // A >= eps >= 0: the guard band, then the reciprocal-free decisions
+    const float aneg = __fmul_rn(A, -0x1p-20f), ahi = __fmaf_rn(A, 0x1p-19f, A);
+    const float u = __fmaf_rn(p.c.x, pz, __fmaf_rn(p.b.w, py, __fmul_rn(p.b.z, px)));
+    if (u < aneg || u > ahi) return false;
+    const float v = __fmaf_rn(r.dz, p.c.w, __fmaf_rn(r.dy, p.c.z, __fmul_rn(r.dx, p.c.y)));
+    if (v < aneg || v > ahi) return false;
+    return cull_tail(A, u, v, p.d.x, r.len, eps, ahi);
 }
 
 // hit() from the packed triangle (v0, e1, e2) and the ray origin.
