@@ -266,6 +266,13 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
 
     unsigned long long tests = 0;
     bool timed_out = false;
+    // with one source per block (the automatic shape for few sources) the lane's
+    // ray is formed once instead of once per tile
+    Ray r1 = Ray{0.f, 0.f, 0.f, 0.f};
+    if (nsrc == 1 && (pending & 1u)) {
+        const float* so = p.src_pos + 3 * src_index(0);
+        r1 = vis_ray<CULL>(so[0], so[1], so[2], ex, ey, ez);
+    }
     int k = 0;
     for (; k < ntiles; ++k) {
         if (!__syncthreads_or(pending != 0)) break;
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(kThreads) brute_stage_kernel(const StageParams
             const bool mine = (pending >> s) & 1u;
             if (!__syncthreads_or(mine)) continue;
             if (mine) {
-                const Ray r = vis_ray<CULL>(ox, oy, oz, ex, ey, ez);
+                const Ray r = nsrc == 1 ? r1 : vis_ray<CULL>(ox, oy, oz, ex, ey, ez);
                 int j = 0;
                 bool hitany = false;
                 for (; j < cnt; ++j) {
