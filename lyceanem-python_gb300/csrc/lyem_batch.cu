@@ -172,7 +172,7 @@ __device__ void vis_item(const BatchParams& P, const DevScene& S, const GridView
         ez = __ldg(kpos + 3 * ms + 2);
     }
     unsigned long long vis = 0;
-    unsigned int tests = 0;  // per lane: at most 64 rays, far below 2^32 tests
+    unsigned int tests = 0;  // diagnostic count of one lane (64 rays at most); wraps only past 2^32 tests
     Walk w;
     for (int s = 0; s < nsrc; ++s) {
         if (!ok) continue;

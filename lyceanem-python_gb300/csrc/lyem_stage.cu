@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
         ex = p.snk_pos[3 * (long long)m]; ey = p.snk_pos[3 * (long long)m + 1]; ez = p.snk_pos[3 * (long long)m + 2];
     }
     unsigned long long blocked = 0;
-    unsigned int tests = 0;  // per lane: at most 64 rays, so the count stays far below 2^32
+    unsigned int tests = 0;  // diagnostic count of one lane (64 rays at most); wraps only past 2^32 tests
     Walk w;
     if (MODE == kTwoPhase16 || MODE == kTwoPhase12) {
         __shared__ int s_hint[kGridMaxChunk];
