@@ -101,7 +101,21 @@ def parse():
                     help="sources per thread block of the pair stages (0 = automatic)")
     ap.add_argument("--traversal", type=int, default=0,
                     help="grid schedule of the pair stages (0 = automatic; see lyem_pair_stage in include/lyem.h)")
+    ap.add_argument("--array-traversal", type=int, default=-1,
+                    help="grid schedule of the two stages that start at the array elements (-1 = the model layer's "
+                         "choice, propagation.source_schedule, unless --traversal is given)")
     return ap.parse_args()
+
+
+def array_schedule(args, src, grid):
+    """Grid schedule of the stages that start at the array elements: --array-traversal, else --traversal when
+    given, else the model layer's choice (the transposed schedule for a compact source set)."""
+    from lyceanem_gb300 import propagation as P
+    if args.array_traversal >= 0:
+        return args.array_traversal
+    if args.traversal != 0:
+        return args.traversal
+    return P.source_schedule(src, grid)
 
 
 def workload_scene(name):
@@ -238,10 +252,11 @@ def run_ours(args, rank, world):
         grid = P.UniformGrid(tris, cell=s.cell)
         o_scat = P.spatial_order(scat)  # scatter points are traced in Morton order
         o_snk = P.direction_order(snk, grid.centre)  # sinks in direction order from the scene
+        ta = array_schedule(args, s.src, grid)
         out = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=grid, counters=c_all, snk_visible=v_dir,
-                           snk_order=o_snk, traversal=args.traversal, src_chunk=args.src_chunk).sink
+                           snk_order=o_snk, traversal=ta, src_chunk=args.src_chunk).sink
         e_p = P.pair_stage(src, E, scat, scat_n, beta=beta, grid=grid, counters=c_all,
-                           snk_visible=v_in, snk_order=o_scat, traversal=args.traversal,
+                           snk_visible=v_in, snk_order=o_scat, traversal=ta,
                            src_chunk=args.src_chunk).sink
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
@@ -792,16 +807,17 @@ def run_parity(args, s):
     src, E = t(s.src), t(s.E)
     yk, ykn = t(snk), t(snk_n)
     o_snk = P.direction_order(yk, grid.centre) if grid is not None else None
-    r0 = P.pair_stage(src, E, yk, ykn, want_mask=True, snk_order=o_snk, **kw)
+    ta = array_schedule(args, s.src, grid)
+    r0 = P.pair_stage(src, E, yk, ykn, want_mask=True, snk_order=o_snk, traversal=ta, **kw)
     field = r0.sink.clone()
     stages = [("direct", s.src, snk, r0)]
     if scat.shape[0]:
         pk, pkn = t(scat), t(scat_n)
         o_scat = P.spatial_order(pk)
-        r1 = P.pair_stage(src, E, pk, pkn, want_mask=True, snk_order=o_scat, **kw)
+        r1 = P.pair_stage(src, E, pk, pkn, want_mask=True, snk_order=o_scat, traversal=ta, **kw)
         e_p = r1.sink
         r2 = P.pair_stage(pk, e_p, yk, ykn, src_W=e_p, sink_out=field, accumulate=True, want_mask=True,
-                          src_order=o_scat, snk_order=o_snk, **kw)
+                          src_order=o_scat, snk_order=o_snk, traversal=args.traversal, **kw)
         stages += [("source_scatter", s.src, scat, r1), ("scatter_sink", scat, snk, r2)]
     gpu_masks = {name: r.mask().cpu().numpy() for name, _, _, r in stages}
     field = field.cpu().numpy()

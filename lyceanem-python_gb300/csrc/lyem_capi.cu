@@ -337,6 +337,7 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
         return LYEM_ERR_INVALID;
     int chunk = src_chunk > 0 ? src_chunk : auto_src_chunk(n_src, n_snk, use_grid);
     chunk = std::min(chunk, use_grid ? grid_max_src_chunk() : brute_max_src_chunk());
+    if (use_grid && traversal == 38) chunk = transposed_src_chunk();  // one lane per source of a chunk
     if ((n_snk + stage_block_threads() - 1) / stage_block_threads() > 0x7fffffffLL) return LYEM_ERR_OVERFLOW;
     const size_t need = stage_ws_bytes(n_src, n_snk, chunk);
     if (!d_ws || ws_bytes < need) return LYEM_ERR_WORKSPACE;
@@ -380,13 +381,14 @@ LYEM_API int lyem_pair_stage(const float* d_src_pos, const float* d_src_E, const
     p.src_order = d_src_order;
     p.snk_order = d_snk_order;
     const bool two_phase = (traversal >= 101 && traversal <= 164) || (traversal >= 201 && traversal <= 264);
-    if ((traversal < 0 || traversal > 36) && !two_phase) return LYEM_ERR_INVALID;
+    if ((traversal < 0 || traversal > 38 || traversal == 37) && !two_phase) return LYEM_ERR_INVALID;
     static const int kCapped[3] = {-10, -12, -16};  // traversal 34, 35, 36
     if (two_phase) {
         p.refill_lanes = traversal < 200 ? -116 : -112;
         p.near_dist = (float)(traversal % 100) * (use_grid ? grid_cell : 1.f);
     } else {
-        p.refill_lanes = traversal == 0 ? -16 : traversal == 1 ? 0 : traversal <= 33 ? traversal - 1 : kCapped[traversal - 34];
+        p.refill_lanes = traversal == 0 ? -16 : traversal == 1 ? 0 : traversal <= 33 ? traversal - 1
+                         : traversal == 38 ? -38 : kCapped[traversal - 34];
     }
     if (d_mask_bits && d_snk_order)  // permuted sinks set their mask bits one by one
         LYEM_CK(cudaMemsetAsync(d_mask_bits, 0, sizeof(uint32_t) * (size_t)n_src * (size_t)p.mask_words, s));

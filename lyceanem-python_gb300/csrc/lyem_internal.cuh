@@ -93,6 +93,7 @@ int stage_block_threads();
 int auto_src_chunk(long long n_src, long long n_snk, bool grid);
 int brute_max_src_chunk();
 int grid_max_src_chunk();
+int transposed_src_chunk();  // sources per block of the transposed grid schedule (traversal 38)
 
 // Beam sweep on the tensor cores (lyem_sweep_tc.cu).  Operand buffers start
 // with a header of kSweepHeaderBytes holding the power-of-two scales (floats

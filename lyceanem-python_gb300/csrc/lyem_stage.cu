@@ -130,6 +130,7 @@ constexpr int kGridMaxChunk = 64;   // one bit per source in a 64-bit mask
 int stage_block_threads() { return kThreads; }
 int brute_max_src_chunk() { return kBruteMaxChunk; }
 int grid_max_src_chunk() { return kGridMaxChunk; }
+int transposed_src_chunk() { return 32; }
 
 struct BruteSmem {
     float4 raw[2][kTile * 3];
@@ -553,6 +554,109 @@ __global__ void __launch_bounds__(kThreads, MODE == kLockstep10 ? 10 : (MODE == 
     flush_block(p, m, m_ok, acc, vis_count, tests);
 }
 
+// Transposed grid stage (traversal 38).  The lanes of a warp are the 32
+// sources of the block's chunk, and each warp traces its 32 sinks one after
+// the other, so the 32 rays a warp walks together end at the same sink.  When
+// the sources are the elements of an array (millimetres apart) those rays cross
+// the same cells and test the same triangles, where a warp of the lockstep
+// schedule holds 32 directions from one source (a CPU model of the walk on the
+// 28 GHz scene: 78.5 instead of 124.8 test iterations per 32 array rays).  The
+// field of each sink is summed over the warp's lanes in a fixed butterfly order
+// and lane 0 writes the chunk's partial sum of that sink.
+constexpr int kTChunk = 32;
+
+template <bool CULL, bool WEIGHTED, bool PAIR_OUT, bool MASK_OUT, bool COUNT>
+__global__ void __launch_bounds__(kThreads, 16) grid_transposed_kernel(const StageParams p) {
+    const unsigned full = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long chunk = p.chunk_base + (long long)blockIdx.y;
+    const int n0 = (int)(chunk * kTChunk);
+    const int nsrc = (int)p.n_src - n0 < kTChunk ? (int)p.n_src - n0 : kTChunk;
+    const bool n_ok = lane < nsrc;
+    const int n = n_ok ? (p.src_order ? p.src_order[n0 + lane] : n0 + lane) : 0;
+    // each source's own-surface triangle (one warp per source), tried before the walk
+    __shared__ int s_hint[kTChunk];
+    for (int s = warp; s < nsrc; s += kThreads / 32) {
+        const int ns = p.src_order ? p.src_order[n0 + s] : n0 + s;
+        const float* so = p.src_pos + 3 * (long long)ns;
+        const int h = warp_nearest_ref(p, so[0], so[1], so[2]);
+        if (lane == 0) s_hint[s] = h;
+    }
+    __syncthreads();
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    if (n_ok) {
+        const float* so = p.src_pos + 3 * (long long)n;
+        ox = so[0]; oy = so[1]; oz = so[2];
+    }
+    const int hint = n_ok ? s_hint[lane] : -1;
+    const int ms0 = (int)blockIdx.x * kThreads + warp * 32;  // the warp's first sink slot
+    unsigned vis_mask = 0;                                    // bit k: this lane's source sees slot ms0 + k
+    unsigned int tests = 0;
+    Walk w;
+    for (int k = 0; k < 32; ++k) {
+        const int ms = ms0 + k;
+        if (ms >= p.n_snk) break;  // the same in every lane
+        const int m = p.snk_order ? p.snk_order[ms] : ms;
+        const float ex = p.snk_pos[3 * (long long)m], ey = p.snk_pos[3 * (long long)m + 1],
+                    ez = p.snk_pos[3 * (long long)m + 2];
+        bool vis = n_ok;  // untested pairs (the skipped diagonal, segments off the grid) are visible
+        if (n_ok && !(p.skip_diag && n == m)) {
+            walk_ray<CULL>(w, ox, oy, oz, ex, ey, ez);
+            bool hit = false;
+            if (hint >= 0) {
+                if (COUNT) ++tests;
+                hit = walk_test_ref<CULL>(p, w, hint);
+            }
+            if (!hit && walk_setup(p, w)) {
+                while (!hit) {
+                    while (w.q < w.q1) {
+                        if (COUNT) ++tests;
+                        if (walk_test<CULL>(p, w)) { hit = true; break; }
+                    }
+                    if (hit || !walk_step(p, w, &g_device_error)) break;
+                }
+            }
+            vis = !hit;
+        }
+        if (vis) {
+            vis_mask |= 1u << k;
+            if (MASK_OUT && p.snk_order) atomicOr(p.mask_bits + (long long)n * p.mask_words + (m >> 5), 1u << (m & 31));
+        }
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float nx = p.snk_nrm[3 * (long long)m], ny = p.snk_nrm[3 * (long long)m + 1],
+                    nz = p.snk_nrm[3 * (long long)m + 2];
+        pair_epilogue<WEIGHTED, PAIR_OUT>(p, n, m, n_ok, vis, ox, oy, oz, ex, ey, ez, nx, ny, nz, acc);
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(full, acc[c], o);
+        const unsigned b = __ballot_sync(full, vis);
+        if (lane == 0) {
+            float2* dst = reinterpret_cast<float2*>(p.partial + 6 * (chunk * p.n_snk + m));
+            dst[0] = make_float2(acc[0], acc[1]);
+            dst[1] = make_float2(acc[2], acc[3]);
+            dst[2] = make_float2(acc[4], acc[5]);
+            if (p.snk_visible && b) atomicAdd(p.snk_visible + m, __popc(b));
+        }
+    }
+    if (n_ok) {
+        if (MASK_OUT && !p.snk_order && ms0 < p.n_snk) p.mask_bits[(long long)n * p.mask_words + (ms0 >> 5)] = vis_mask;
+        if (p.src_visible && vis_mask) atomicAdd(p.src_visible + n, __popc(vis_mask));
+    }
+    if (p.counters) {
+        unsigned long long v = __popc(vis_mask), t = tests;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v += __shfl_down_sync(full, v, o);
+            t += __shfl_down_sync(full, t, o);
+        }
+        if (lane == 0) {
+            if (v) atomicAdd(p.counters + 0, v);
+            if (t) atomicAdd(p.counters + 1, t);
+        }
+    }
+}
+
 __global__ void reduce_partials_kernel(const float* __restrict__ partial, long long n_chunks, long long n_elem,
                                        float* __restrict__ out, int accumulate) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_elem;
@@ -579,6 +683,11 @@ static cudaError_t launch_t(const StageParams& p0, cudaStream_t stream) {
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase16><<<grid, kThreads, qbytes, stream>>>(p);
                 else
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kTwoPhase12><<<grid, kThreads, qbytes, stream>>>(p);
+            } else if (p.refill_lanes == -38) {
+                if (p.counters)
+                    grid_transposed_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, true><<<grid, kThreads, 0, stream>>>(p);
+                else
+                    grid_transposed_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, false><<<grid, kThreads, 0, stream>>>(p);
             } else if (p.refill_lanes == -16) {
                 if (p.counters)
                     grid_stage_kernel<CULL, WEIGHTED, PAIR_OUT, MASK_OUT, kLockstep16><<<grid, kThreads, 0, stream>>>(p);

@@ -60,11 +60,13 @@ def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=Non
     # caller's order.
     snk = P._points(snk)
     o_snk = _sink_order(dev, snk)
-    out = P.pair_stage(src, E, snk, snk_n, snk_order=o_snk, **kw).sink
+    # the stages that start at the sources take the transposed schedule when the sources are compact (an array)
+    ts = P.source_schedule(src, dev.grid)
+    out = P.pair_stage(src, E, snk, snk_n, snk_order=o_snk, traversal=ts, **kw).sink
     if scattering >= 1 and scat is not None and len(scat):
         scat = P._points(scat)
         o_scat = P.spatial_order(scat)
-        e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, **kw).sink
+        e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, traversal=ts, **kw).sink
         P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat,
                      snk_order=o_snk, **kw)
     return out

@@ -181,7 +181,9 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     pairs = torch.empty((N, M, 3), dtype=torch.complex64, device=dev) if want_pairs else None
     words = (M + 31) // 32
     mbits = torch.empty((N, words), dtype=torch.int32, device=dev) if want_mask else None
-    need = lib.lyem_pair_stage_workspace(N, M, T, int(grid is not None), int(src_chunk))
+    # the transposed schedule (traversal 38) takes 32 sources per block, whatever src_chunk says
+    wchunk = 32 if (grid is not None and traversal == 38) else int(src_chunk)
+    need = lib.lyem_pair_stage_workspace(N, M, T, int(grid is not None), wchunk)
     if workspace is None or workspace.numel() < need:
         workspace = _ws(need, dev)
     st = lib.lyem_pair_stage(_p(sp), _p(torch.view_as_real(E)), _p(None if W is None else torch.view_as_real(W)), N,
@@ -205,6 +207,28 @@ def spatial_order(points):
         ws = _ws(lib.lyem_spatial_order_workspace(n), pts.device)
         check(lib.lyem_spatial_order(_p(pts), n, _p(out), _p(ws), ws.numel(), _stream()), "spatial_order")
     return out
+
+
+def source_schedule(src, grid):
+    """Grid schedule for a source set: the transposed one (traversal 38: the lanes of a warp are 32 sources,
+    the warp walks one sink at a time) when every source lies within one grid cell of every other (the
+    elements of an array), so that a warp's rays to a sink cross the same cells; otherwise the default (0).
+    A device tensor is reduced on the device (one small synchronisation)."""
+    if grid is None:
+        return 0
+    if isinstance(src, torch.Tensor):
+        a = src.reshape(-1, 3)
+        if a.shape[0] == 0:
+            return 0
+        lo, hi = torch.aminmax(a.float(), dim=0)
+        ext = (hi - lo).double().cpu().numpy()
+    else:
+        import numpy as np
+        a = np.asarray(src, np.float64).reshape(-1, 3)
+        if a.shape[0] == 0:
+            return 0
+        ext = a.max(0) - a.min(0)
+    return 38 if float((ext ** 2).sum()) ** 0.5 <= grid.cell else 0
 
 
 def direction_order(points, centre):

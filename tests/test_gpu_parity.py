@@ -324,9 +324,10 @@ def test_bounce_config_full_geometry_slice():
     assert rel_err(field.cpu().numpy(), ref) < FIELD_TOL
 
 
-@pytest.mark.parametrize("traversal", [36, 1, 102, 104, 203])
+@pytest.mark.parametrize("traversal", [36, 38, 1, 102, 104, 203])
 def test_grid_schedules_bit_identical_full_geometry(traversal):
-    """Every grid schedule (lockstep capped and uncapped; two phases split at 2, 4 and 3 cells) gives the
+    """Every grid schedule (lockstep capped and uncapped; the transposed schedule; two phases split at 2, 4 and 3
+    cells) gives the
     oracle's masks and the same sink field on the full 28 GHz geometry (slice of sinks and scatter points,
     the benchmarked processing orders), for the array-to-sink and scatter-to-sink stages, with and without
     the test counters."""
@@ -348,7 +349,10 @@ def test_grid_schedules_bit_identical_full_geometry(traversal):
         ref = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=36, **kw)
         r = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=traversal, **kw)
         assert np.array_equal(r.mask().cpu().numpy(), og.mask(a, b))
-        assert torch.equal(r.sink, ref.sink)
+        if traversal == 38:  # 32 sources per block, summed across the warp: another summation order
+            assert rel_err(r.sink.cpu().numpy(), ref.sink.cpu().numpy()) < 1e-6
+        else:
+            assert torch.equal(r.sink, ref.sink)
         # with counters (the default schedule then runs its counting variant): same results
         cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
         rc = P.pair_stage(a, E, b, bn, beta=beta, grid=grid, want_mask=True, traversal=traversal, counters=cnt, **kw)
