@@ -36,14 +36,15 @@ class SinkField(torch.autograd.Function):
         E_src = (pol * a.reshape(-1, 1)).contiguous()
         kw = dict(beta=beta, alpha=alpha, grid=grid, tris=tris, self_to_self=self_to_self, want_mask=True)
         o_snk = P.direction_order(y, grid.centre) if grid is not None else None
-        r0 = P.pair_stage(x, E_src, y, snk_n, snk_order=o_snk, **kw)
+        ts = P.source_schedule(x, grid)  # the transposed schedule for a compact element set
+        r0 = P.pair_stage(x, E_src, y, snk_n, snk_order=o_snk, traversal=ts, **kw)
         E = r0.sink
         have_scat = scat is not None and scat.shape[0] > 0
         if have_scat:
             scat = P._points(scat)
             scat_n = P._points(scat_n)
             order = P.spatial_order(scat)
-            r1 = P.pair_stage(x, E_src, scat, scat_n, snk_order=order, **kw)
+            r1 = P.pair_stage(x, E_src, scat, scat_n, snk_order=order, traversal=ts, **kw)
             w = r1.sink
             r2 = P.pair_stage(scat, w, y, snk_n, src_W=w, sink_out=E, accumulate=True, src_order=order,
                               snk_order=o_snk, **kw)
