@@ -173,7 +173,8 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * and walked to their end 32 at a time; 38 = transposed: the lanes of a warp
  * are 32 sources (32 sources per block, whatever src_chunk says: query the
  * workspace with src_chunk = 32) and the warp walks one sink at a time, which
- * pays when the sources are compact (the elements of an array); 0 = automatic
+ * pays when the sources are compact (the elements of an array) and no per-pair
+ * output is asked for (its d_pair_out writes are strided); 0 = automatic
  * (currently 36).  Every schedule gives the same masks; the transposed one
  * sums each sink's field in another order (same result to FP32 rounding). */
 LYEM_API size_t lyem_pair_stage_workspace(int64_t n_src, int64_t n_snk, int64_t n_tris, int32_t use_grid,

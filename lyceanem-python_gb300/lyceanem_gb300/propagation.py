@@ -213,7 +213,8 @@ def source_schedule(src, grid):
     """Grid schedule for a source set: the transposed one (traversal 38: the lanes of a warp are 32 sources,
     the warp walks one sink at a time) when every source lies within one grid cell of every other (the
     elements of an array), so that a warp's rays to a sink cross the same cells; otherwise the default (0).
-    A device tensor is reduced on the device (one small synchronisation)."""
+    Meant for the source-summed field: with a per-pair network output the transposed schedule's pair writes
+    are strided.  A device tensor is reduced on the device (one small synchronisation)."""
     if grid is None:
         return 0
     if isinstance(src, torch.Tensor):
