@@ -453,6 +453,12 @@ def test_edge_sizes(n_src, n_snk, n_tris):
     g = P.UniformGrid(tris)  # also with no triangles: a one-cell grid whose cell table is empty
     r = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=g, want_mask=True)
     assert np.array_equal(r.mask().cpu().numpy(), om)
+    # the transposed schedule (lanes over up to 32 sources, fewer in a ragged last chunk), with the per-pair output
+    rt = P.pair_stage(src, E, snk, snk_n, beta=beta, grid=g, want_mask=True, want_pairs=True, traversal=38)
+    assert np.array_equal(rt.mask().cpu().numpy(), om)
+    assert rel_err(rt.sink.cpu().numpy(), ref) < FIELD_TOL
+    rb = P.pair_stage(src, E, snk, snk_n, beta=beta, tris=tris, want_pairs=True)
+    assert rel_err(rt.pairs.cpu().numpy(), rb.pairs.cpu().numpy()) < 1e-6
     _no_device_errors()
 
 
@@ -519,7 +525,7 @@ def test_spatial_order_and_ordered_stages():
     assert sorted(o_src.cpu().tolist()) == list(range(150))
     om = O.mask_brute(src, snk, O.pack_triangles(v, f))
     g = P.UniformGrid(tris, cell=0.25)
-    for kw in (dict(tris=tris), dict(grid=g)):
+    for kw in (dict(tris=tris), dict(grid=g), dict(grid=g, traversal=38)):
         a = P.pair_stage(src, E, snk, snk_n, beta=80.0, want_mask=True, want_pairs=True, **kw)
         b = P.pair_stage(src, E, snk, snk_n, beta=80.0, want_mask=True, want_pairs=True, src_order=o_src,
                          snk_order=o_snk, **kw)
