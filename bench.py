@@ -22,7 +22,9 @@ Side legs of the default run, each reported in its own object of the JSON line
 (skipped with --no-<leg>): full-geometry parity against the oracle, the
 direct-path workload (brute force) with its roofline and parity, the
 mixed-precision beam sweep, the adjoint, the batched many-scene launch, the
-end-to-end call through the reference-shaped API, and the CPU baseline.
+model layer's field with and without the opt-in skip of unlit scattering
+points (--no-unlit), the end-to-end call through the reference-shaped API, and
+the CPU baseline.  The headline step traces every scatter->sink ray.
 """
 import argparse
 import json
@@ -93,6 +95,8 @@ def parse():
     ap.add_argument("--batched-cell-scale", type=float, default=0.0,
                     help="grid cell scale k of the batched scenes instead of the autotuner (profiling cases)")
     ap.add_argument("--no-parity", action="store_true", help="skip the full-geometry parity check against the oracle")
+    ap.add_argument("--no-unlit", action="store_true",
+                    help="skip the side leg timing the one-bounce field traced only from lit scattering points")
     ap.add_argument("--no-direct", action="store_true",
                     help="skip the direct-path (8x8 array, brute force) leg of the bounce workload's run")
     ap.add_argument("--sweep-case", choices=["full", "small"], default="full",
@@ -358,6 +362,8 @@ def run_ours(args, rank, world):
         res["batched"] = run_batched(args)
     if rank == 0 and world == 1 and not args.no_direct and args.workload == "bounce":
         res["direct"] = run_direct(args, rank, world)
+    if rank == 0 and world == 1 and not args.no_unlit and args.workload == "bounce":
+        res["skip_unlit"] = run_unlit(args, s)
     if rank == 0 and world == 1 and not args.no_e2e:
         res["e2e"] = run_e2e(args, s, paths)
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -381,6 +387,50 @@ def run_direct(args, rank, world, steps=50, warmup=5):
                                             "ops_per_test", "traffic")},
             "parity": {k: sub["parity"][k] for k in ("sample", "pairs", "mask_mismatches", "edge_pairs",
                                                      "field_rel_err", "ok")}}
+
+
+def run_unlit(args, s, reps=3):
+    """Side leg: the model layer's fused field (models.frequency_domain.sink_field, device-resident scene and
+    grid) with and without skip_unlit, which traces the one bounce only from the scattering points that some
+    source sees.  Each call is timed with CUDA events after an L2 flush; the fields are compared."""
+    import numpy as np
+    import torch
+
+    from lyceanem_gb300 import propagation as P
+    from lyceanem_gb300.models import acceleration_structures as AS
+    from lyceanem_gb300.models.frequency_domain import sink_field
+    beta = 2 * np.pi / s.wavelength
+    dev = AS._DeviceScene(s.verts, s.faces, grid_cell=s.cell)
+    st = type("S", (), {"device": dev})()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out, ms, tests = {}, {}, {}
+    for skip in (False, True):
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        out[skip] = sink_field(st, s.src, s.E, s.snk, s.snk_n, 0.0, beta, s.scat, s.scat_n, scattering=1,
+                               counters=cnt, skip_unlit=skip)
+        tests[skip] = int(cnt[1].item())
+        times = []
+        for _ in range(reps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            sink_field(st, s.src, s.E, s.snk, s.snk_n, 0.0, beta, s.scat, s.scat_n, scattering=1, skip_unlit=skip)
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        ms[skip] = min(times)
+    seen = torch.zeros(s.scat.shape[0], dtype=torch.int32, device="cuda")
+    P.pair_stage(s.src, s.E, s.scat, s.scat_n, beta=beta, grid=dev.grid, snk_visible=seen)
+    st_, flags = P.device_errors()
+    if st_ != 0 or flags != 0:
+        raise RuntimeError(f"device error word {flags:#x}")
+    d = (out[True] - out[False]).abs().max().item() / out[False].abs().max().item()
+    return {"api": "models.frequency_domain.sink_field(scattering=1), scene and grid resident, inputs uploaded "
+                   "per call; best of %d calls, L2 flushed before each" % reps,
+            "ms_full": ms[False], "ms_skip_unlit": ms[True], "speedup": ms[False] / ms[True],
+            "lit_scatter_points": int((seen > 0).sum().item()), "scatter_points": int(s.scat.shape[0]),
+            "tests_full": tests[False], "tests_skip_unlit": tests[True], "field_rel_diff": d}
 
 
 def run_e2e(args, s, paths):

@@ -162,6 +162,13 @@ LYEM_API int lyem_spatial_order(const float *d_points, int64_t n_points, int32_t
  * lyem_spatial_order that set which sources share a thread block and which
  * sinks share a warp; results are unchanged (sink sums are summed in chunk
  * order, so a different source order can change the last bits of the field).
+ * d_src_order may also list a subset: n_src distinct row indices into source
+ * arrays (d_src_pos, d_src_E, d_src_W) that hold more rows.  Only the listed
+ * sources are traced; every per-source output (d_pair_out, d_mask_bits,
+ * d_src_visible) is indexed by the source's row, so it needs as many rows as
+ * the source arrays, and the rows left out are not written.  A source keeps
+ * its row index, so self_to_self = 0 still skips the pair of equal row and
+ * sink index.  Nothing checks the indices: each must be below the row count.
  * src_chunk: sources per thread block (0 = automatic; at most 32 for brute
  * force, 64 for the grid).  traversal (grid only): 1 = all lanes of a warp
  * trace the same source in lockstep; k in 2..33 = each lane moves on to its

@@ -49,9 +49,17 @@ def _sink_order(dev, snk):
 
 
 def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=None, scattering=0, counters=None,
-               cull=True, eps=P.EPSILON):
+               cull=True, eps=P.EPSILON, skip_unlit=False):
     """Fused source-summed sink field (complex64 [M,3] CUDA tensor) of the direct path and,
-    with scattering=1, the one-bounce path, on the current stream."""
+    with scattering=1, the one-bounce path, on the current stream.
+
+    skip_unlit: trace the scatter->sink rays only from the scattering points that
+    at least one source sees.  A point no source sees has a source->scatter field
+    of exactly zero, so every one-bounce path through it contributes exactly zero
+    (the reference forms those paths in S1 @ S2, lyceanem/models/frequency_domain.py:
+    230-260, and their products vanish); the field is the same up to the FP32
+    rounding of the regrouped source sums.  Costs one device->host read (the
+    number of lit points)."""
     dev = structure.device
     kw = dict(tris=dev.tris, grid=dev.grid, alpha=alpha, beta=beta, self_to_self=False, counters=counters, cull=cull,
               eps=eps)
@@ -66,9 +74,19 @@ def sink_field(structure, src, E, snk, snk_n, alpha, beta, scat=None, scat_n=Non
     if scattering >= 1 and scat is not None and len(scat):
         scat = P._points(scat)
         o_scat = P.spatial_order(scat)
-        e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, traversal=ts, **kw).sink
-        P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat,
-                     snk_order=o_snk, **kw)
+        if not skip_unlit:
+            e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, traversal=ts, **kw).sink
+            P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=o_scat,
+                         snk_order=o_snk, **kw)
+            return out
+        seen = torch.zeros(scat.shape[0], dtype=torch.int32, device=scat.device)
+        e_p = P.pair_stage(src, E, scat, scat_n, snk_order=o_scat, traversal=ts, snk_visible=seen, **kw).sink
+        # the lit points in Morton order, passed as a subset order (each keeps its row, so the reference's
+        # untested pair of equal source and sink index stays the same pair)
+        lit = o_scat[seen[o_scat.long()] > 0].contiguous()
+        if lit.numel():
+            P.pair_stage(scat, e_p, snk, snk_n, src_W=e_p, sink_out=out, accumulate=True, src_order=lit,
+                         snk_order=o_snk, **kw)
     return out
 
 
@@ -265,7 +283,7 @@ def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_
                          wavelength=1.0, scattering=0, elements=False, los=True, project_vectors=False,
                          antenna_axes=np.eye(3), multiE=False, alpha=0.0, beta=(np.pi * 2) / 1.0, cuda=False,
                          acceleration_structure=None, chunks=1, permittivity=8.8541878176e-12,
-                         permeability=1.25663706212e-6, grid_cell=None):
+                         permeability=1.25663706212e-6, grid_cell=None, skip_unlit=False):
     """Ex, Ey, Ez at the sinks (elements=False: complex64 [M] each, summed over
     sources) or per element (elements=True: [N, M] each), like the reference.
 
@@ -274,7 +292,11 @@ def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_
     lyceanem/raycasting/rayfunctions.py:37-104, 2624-2680), its path product with
     tangential projection at scatter points and sinks
     (lyceanem/electromagnetics/empropagation.py:1083-1265) and its excitation
-    rules; scattering=2 goes through the explicit path list."""
+    rules; scattering=2 goes through the explicit path list.
+
+    skip_unlit (not in the reference; CUDA branch, source-summed fields): the
+    one-bounce stage traces only from the scattering points that some source
+    sees, as sink_field describes; off by default."""
     del permittivity, permeability
     if not cuda:
         return _numba_branch(aperture_coords, sink_coords, antenna_solid, desired_E_axis, scatter_points, scattering,
@@ -294,7 +316,8 @@ def calculate_scattering(aperture_coords, sink_coords, antenna_solid, desired_E_
     N = src.shape[0]
 
     def fused(E):
-        f = sink_field(acc, src, E, snk, snk_n, alpha, beta, scat, scat_n, scattering, cull=cull, eps=eps)
+        f = sink_field(acc, src, E, snk, snk_n, alpha, beta, scat, scat_n, scattering, cull=cull, eps=eps,
+                       skip_unlit=skip_unlit)
         f = f.cpu().numpy()
         return f[:, 0], f[:, 1], f[:, 2]
 

@@ -152,6 +152,9 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     per source / per sink.
     src_order / snk_order (int32, e.g. from spatial_order) set the processing
     order only: which sources share a thread block and which sinks a warp.
+    A src_order shorter than src_pos selects a subset: only the sources it
+    lists (distinct rows) are traced, and the per-source outputs keep one row
+    per row of src_pos (zero for the rows left out).
     src_chunk / traversal choose the launch shape and the ray schedule of the
     grid kernel (0 = automatic; see lyem_pair_stage in include/lyem.h).
     Visibility uses `grid` (a UniformGrid) if given, else brute force over
@@ -159,9 +162,12 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     n == m (lyceanem/src/raycasting_brute_force.cuh:27)."""
     sp = _points(src_pos)
     dev = sp.device
-    N = sp.shape[0]
-    E = _cvec(src_E, N)
-    W = None if src_W is None else _cvec(src_W, N)
+    rows = sp.shape[0]
+    N = rows if src_order is None else int(src_order.shape[0])
+    if N > rows:
+        raise ValueError(f"src_order lists {N} sources for {rows} rows")
+    E = _cvec(src_E, rows)
+    W = None if src_W is None else _cvec(src_W, rows)
     tp = _points(snk_pos)
     tn = _points(snk_nrm)
     M = tp.shape[0]
@@ -178,9 +184,10 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     if sink_out is None:
         sink_out = torch.empty((M, 3), dtype=torch.complex64, device=dev)
         accumulate = False
-    pairs = torch.empty((N, M, 3), dtype=torch.complex64, device=dev) if want_pairs else None
+    alloc = torch.empty if N == rows else torch.zeros  # rows left out of a subset stay zero
+    pairs = alloc((rows, M, 3), dtype=torch.complex64, device=dev) if want_pairs else None
     words = (M + 31) // 32
-    mbits = torch.empty((N, words), dtype=torch.int32, device=dev) if want_mask else None
+    mbits = alloc((rows, words), dtype=torch.int32, device=dev) if want_mask else None
     # the transposed schedule (traversal 38) takes 32 sources per block, whatever src_chunk says
     wchunk = 32 if (grid is not None and traversal == 38) else int(src_chunk)
     need = lib.lyem_pair_stage_workspace(N, M, T, int(grid is not None), wchunk)
@@ -195,7 +202,7 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
                              _p(src_visible), _p(snk_visible), _p(src_order), _p(snk_order), int(src_chunk),
                              int(traversal), _p(workspace), workspace.numel(), _stream())
     check(st, "pair_stage")
-    return StageResult(sink_out, pairs, mbits, counters, N, M)
+    return StageResult(sink_out, pairs, mbits, counters, rows, M)
 
 
 def spatial_order(points):

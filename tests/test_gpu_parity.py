@@ -282,6 +282,15 @@ def test_bounce_scene_reduced_vs_oracle():
     og = O.Grid(otris, s.cell)
     ref, e_p = O.onebounce_sink_field(s.src, s.E, s.snk, s.snk_n, s.scat, s.scat_n, 0.0, beta, grid=og)
     assert rel_err(E, ref) < FIELD_TOL
+    # tracing the one bounce only from the scattering points some source sees: the same field, fewer tests
+    seen = og.mask(s.src, s.scat).any(0)
+    seen[:min(len(s.src), len(s.scat))] = True  # self_to_self=False: the pair n == p is untested, so visible
+    assert 0 < seen.sum() < len(seen)
+    cnt_l = torch.zeros(2, dtype=torch.int64, device="cuda")
+    El = sink_field(type("S", (), {"device": dev})(), s.src, s.E, s.snk, s.snk_n, 0.0, beta, s.scat, s.scat_n,
+                    scattering=1, counters=cnt_l, skip_unlit=True).cpu().numpy()
+    assert rel_err(El, ref) < FIELD_TOL and rel_err(El, E) < 1e-6
+    assert 0 < int(cnt_l[1]) < int(cnt[1])
     # stage masks are bit-exact against the oracle
     for a, an, b, bn in ((s.src, s.src_n, s.snk, s.snk_n), (s.src, s.src_n, s.scat, s.scat_n),
                          (s.scat, s.scat_n, s.snk, s.snk_n)):
@@ -532,6 +541,40 @@ def test_spatial_order_and_ordered_stages():
         assert np.array_equal(b.mask().cpu().numpy(), om)
         assert torch.equal(a.pairs, b.pairs)
         assert rel_err(b.sink.cpu().numpy(), a.sink.cpu().numpy()) < 1e-6
+    _no_device_errors()
+
+
+@pytest.mark.parametrize("mode", ["brute", "grid", "grid38"])
+def test_source_subset_order(mode):
+    """A src_order shorter than the source arrays traces only the listed rows: their mask rows, per-pair
+    rows and visible counts are the full stage's, the other rows stay zero, and the field is the oracle's sum
+    over the listed sources.  Rows 0 and 3 are listed, so the untested pairs (0, 0) and (3, 3) of
+    self_to_self=False stay with their rows."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(53, n_src=70, n_snk=90, n_tris=300)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    om = O.mask_brute(src, snk, O.pack_triangles(v, f))
+    rng = np.random.default_rng(5)
+    sub = np.unique(np.concatenate([rng.choice(70, size=37, replace=False), [0, 3]]))[::-1].copy()
+    keep = np.zeros(70, bool)
+    keep[sub] = True
+    if mode == "brute":
+        kw = dict(tris=tris)
+    else:
+        kw = dict(grid=P.UniformGrid(tris), traversal=38 if mode == "grid38" else 0)
+    vis = torch.zeros(70, dtype=torch.int32, device="cuda")
+    order = torch.from_numpy(sub.astype(np.int32)).cuda()
+    r = P.pair_stage(src, E, snk, snk_n, beta=50.0, want_mask=True, want_pairs=True, src_visible=vis,
+                     src_order=order, **kw)
+    full = P.pair_stage(src, E, snk, snk_n, beta=50.0, want_mask=True, want_pairs=True, **kw)
+    mk = r.mask().cpu().numpy()
+    assert mk.shape == om.shape
+    assert np.array_equal(mk[keep], om[keep]) and not mk[~keep].any()
+    assert np.array_equal(vis.cpu().numpy(), np.where(keep, om.sum(1), 0))
+    pr, pf = r.pairs.cpu().numpy(), full.pairs.cpu().numpy()
+    assert np.all(pr[~keep] == 0) and np.array_equal(pr[keep], pf[keep])
+    ref = O.sink_field(src, E, snk, snk_n, 0.0, 50.0, mask=om & keep[:, None])
+    assert rel_err(r.sink.cpu().numpy(), ref) < FIELD_TOL
     _no_device_errors()
 
 
