@@ -137,6 +137,17 @@ class StageResult:
         return out.bool()
 
 
+def _check_buffer(name, t, dtype, n, exact):
+    """Caller-provided device buffer of the stage: a contiguous 1-D CUDA tensor of `dtype` with exactly
+    (exact) or at least n entries; the kernels index it without bounds checks."""
+    if t is None:
+        return
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.dim() == 1 and t.is_contiguous()):
+        raise ValueError(f"{name} must be a contiguous 1-D {dtype} CUDA tensor")
+    if (t.numel() != n) if exact else (t.numel() < n):
+        raise ValueError(f"{name} has {t.numel()} entries, {'' if exact else 'at least '}{n} needed")
+
+
 def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, grid=None, src_W=None,
                self_to_self=False, cull=True, eps=EPSILON, sink_out=None, accumulate=False, want_pairs=False,
                want_mask=False, counters=None, src_visible=None, snk_visible=None, src_order=None, snk_order=None,
@@ -171,6 +182,11 @@ def pair_stage(src_pos, src_E, snk_pos, snk_nrm, *, beta, alpha=0.0, tris=None, 
     tp = _points(snk_pos)
     tn = _points(snk_nrm)
     M = tp.shape[0]
+    _check_buffer("src_order", src_order, torch.int32, N, True)
+    _check_buffer("snk_order", snk_order, torch.int32, M, True)
+    _check_buffer("src_visible", src_visible, torch.int32, rows, False)
+    _check_buffer("snk_visible", snk_visible, torch.int32, M, False)
+    _check_buffer("counters", counters, torch.int64, 2, False)
     if grid is not None:
         tri_t, T = None, 0
         cs, ct, cb = grid.cell_start, grid.cell_tris, grid.cell_box

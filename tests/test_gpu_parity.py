@@ -471,6 +471,27 @@ def test_edge_sizes(n_src, n_snk, n_tris):
     _no_device_errors()
 
 
+def test_stage_buffer_checks():
+    """Caller buffers of the wrong type or length are refused before any launch (the kernels index them
+    without bounds checks)."""
+    P = _P()
+    src, snk, snk_n, v, f, E = random_scene(3, n_src=6, n_snk=40, n_tris=50)
+    tris = P.pack_triangles(torch.from_numpy(v), torch.from_numpy(f))
+    cu = dict(device="cuda")
+    bad = [dict(src_order=torch.arange(6, dtype=torch.int64, **cu)),     # int64 order
+           dict(src_order=torch.arange(7, dtype=torch.int32, **cu)),     # more entries than rows
+           dict(snk_order=torch.arange(39, dtype=torch.int32, **cu)),    # not a permutation's length
+           dict(snk_visible=torch.zeros(39, dtype=torch.int32, **cu)),   # too short
+           dict(src_visible=torch.zeros(6, dtype=torch.int32)),          # host tensor
+           dict(counters=torch.zeros(2, dtype=torch.int32, **cu))]       # int32 counters
+    for kw in bad:
+        with pytest.raises(ValueError):
+            P.pair_stage(src, E, snk, snk_n, beta=10.0, tris=tris, **kw)
+    r = P.pair_stage(src, E, snk, snk_n, beta=10.0, tris=tris, snk_visible=torch.zeros(40, dtype=torch.int32, **cu))
+    assert r.sink.shape == (40, 3)
+    _no_device_errors()
+
+
 def test_empty_inputs():
     P = _P()
     z = np.zeros((0, 3), np.float32)
